@@ -1,0 +1,407 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 LSD radix-sort pass library.
+
+Workload (the headline configuration): one step = one full LSD sort
+(lsb_sort_pairs, the reference's mySort, mpi/mpi_lsbsort.cpp:592-597) of
+2^30 16-byte {uint64 key, uint64 value} elements, keys uniform from the seeded
+splitmix64 stream, value = index, 16-bit digits (the reference's RADIX, 4
+passes). The input is restored from a resident copy before every step (not
+timed), so every step sorts the same unsorted 16 GiB array; arrays are far
+larger than L2, and the restore copy itself sweeps L2.
+
+Prints ONE JSON line (rank 0):
+  value        M elements/s, whole job, inputs resident in HBM, CUDA events
+  e2e          same metric through the host-buffer C-ABI call
+               (lsb_sort_pairs_host: H2D copy + sort + D2H copy per step)
+  roofline     dominant kernel: algorithmic bytes per launch / mean launch time,
+               against the measured HBM copy bandwidth (MEASURED_PEAKS.json)
+  cpu_baseline the oracle's port of the reference algorithm on the host cores
+               (bounded sample), rank 0 at N=1 only
+  clocks       SM clock samples taken during the timed region
+
+--impl reference times the reference algorithm on the host cores instead
+(see cpu_arm below). --gpus N (torchrun) runs N independent replicas, one
+2^30 sort per GPU per step ("replicas only": the single-array sort does not
+shard across the GPUs of one box here), value = elements of all ranks / max
+rank time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "distributed-lsb_gb300")
+for _p in (ROOT, PKG):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "M 16-byte elems sorted/s on 1 GB300 (2^30, HBM-roofline %); batched vs plain; p50/p99"
+UNIT = "M elem/s"
+DIST_NAMES = {"uniform": 0, "low32": 1, "zipf": 2, "equal": 3, "nearly_sorted": 4}
+
+
+def algorithmic_bytes_per_element(digit_bits: int, passes_run: int) -> int:
+    """One key read for the digit counts + 32 B (read 16, write 16) per pass run."""
+    return 8 + 32 * passes_run
+
+
+def args_parse(argv=None):
+    p = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", choices=["native", "reference"], default="native")
+    p.add_argument("--n", type=int, default=1 << 30)
+    p.add_argument("--digit-bits", type=int, default=16)
+    p.add_argument("--dist", choices=sorted(DIST_NAMES), default="uniform")
+    p.add_argument("--e2e-steps", type=int, default=3)
+    p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
+    p.add_argument("--no-extra", action="store_true", help="skip the 8-bit-digit side measurement")
+    p.add_argument("--cpu-sample", type=int, default=1 << 26)
+    return p.parse_args(argv)
+
+
+# ---------------------------------------------------------------------------
+# ranks
+
+class Ranks:
+    """Process-group plumbing for --gpus N (one process per GPU, env:// rendezvous)."""
+
+    def __init__(self):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+        self.dist = None
+        if self.world > 1:
+            import torch
+            import torch.distributed as dist
+
+            backend = "nccl" if torch.cuda.is_available() else "gloo"
+            if backend == "nccl":
+                torch.cuda.set_device(self.local_rank)
+            dist.init_process_group(backend=backend)
+            self.dist = dist
+            self.backend = backend
+
+    def barrier(self):
+        if self.dist is not None:
+            self.dist.barrier()
+
+    def max(self, x: float) -> float:
+        if self.dist is None:
+            return x
+        import torch
+
+        dev = "cuda" if self.backend == "nccl" else "cpu"
+        t = torch.tensor([x], dtype=torch.float64, device=dev)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.dist is not None:
+            self.dist.destroy_process_group()
+
+
+# ---------------------------------------------------------------------------
+# clocks
+
+class ClockSampler:
+    """nvidia-smi sampling (200 ms) of SM clock and throttle reasons during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        with open(self.path) as f:
+            for line in f:
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) < 9:
+                    continue
+                try:
+                    sm.append(float(parts[1]))
+                    smax.append(float(parts[2]))
+                except ValueError:
+                    continue
+                for nm, v in zip(names, parts[5:9]):
+                    if v.lower() == "active":
+                        reasons.add(nm)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def measured_peaks() -> dict:
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return {"hbm_gbs": float(d["hbm_gbs"]), "source": "MEASURED_PEAKS.json (measured)"}
+    return {"hbm_gbs": 6800.0, "source": "fallback 6.8 TB/s"}
+
+
+def committed_traffic(kernel: str, n: int, digit_bits: int):
+    """DRAM bytes per launch from the committed ncu summary, scaled to n."""
+    p = os.path.join(ROOT, "profiles", "traffic.json")
+    if not os.path.exists(p):
+        return None, None
+    with open(p) as f:
+        d = json.load(f)
+    rec = d.get(f"{kernel}/b{digit_bits}")
+    if not rec:
+        return None, None
+    return rec["dram_bytes_per_element"] * n, rec.get("source")
+
+
+# ---------------------------------------------------------------------------
+# the CPU arm and the cpu_baseline leg
+
+def cpu_sort_rate(sample: int, reps: int, warmup: int = 0, budget_s: float = 30.0):
+    """Times the oracle's port of the reference algorithm (all host cores, one
+    simulated MPI rank per thread) on `sample` uniform elements. Returns
+    (M elem/s over the timed reps, per-rep seconds, threads)."""
+    import oracle
+
+    oracle.build(with_ref=False) if not os.path.exists(oracle.ORACLE_SO) else None
+    threads = os.cpu_count() or 1
+    a = oracle.generate(sample, oracle.DIST_UNIFORM, 0)
+    times = []
+    for i in range(warmup + reps):
+        t0 = time.perf_counter()
+        oracle.mysort(a, 16, ranks=threads, threads=threads)
+        dt = time.perf_counter() - t0
+        if i >= warmup:
+            times.append(dt)
+        if sum(times) > budget_s:
+            break
+    return sample * len(times) / sum(times) / 1e6, times, threads
+
+
+def cpu_arm(args, ranks: Ranks):
+    """--impl reference: the reference algorithm on the host cores (the oracle's
+    C port of mpi/mpi_lsbsort.cpp, one simulated rank per thread; the
+    reference's own build needs its source tree, which only the development
+    container has). Each step sorts a bounded sample of the workload."""
+    if ranks.rank != 0:
+        return None
+    sample = args.cpu_sample
+    value, times, threads = cpu_sort_rate(sample, max(args.steps, 1), warmup=args.warmup, budget_s=120.0)
+    ms = 1e3 * statistics.mean(times)
+    return {
+        "impl": "reference",
+        "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": args.gpus,
+        "steps": len(times), "warmup": args.warmup, "ms_per_step": round(ms, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
+        "data": "synthetic",
+        "config": {"workload": f"lsd-sort uniform u64 keys, 16-bit digits, sample of {sample} elements per step",
+                   "n": sample, "digit_bits": 16, "dist": "uniform"},
+        "cpu_baseline": {"value": round(value, 3), "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"{sample} elements x {len(times)} steps"},
+        "e2e": {"value": round(value, 3), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+# ---------------------------------------------------------------------------
+# the GPU arm
+
+def gpu_arm(args, ranks: Ranks):
+    import torch
+
+    import lsb_gb300 as lsb
+
+    torch.cuda.set_device(ranks.local_rank)
+    lsb.build()
+    lsb.load()
+    n, bits = args.n, args.digit_bits
+    dist = DIST_NAMES[args.dist]
+    inp = lsb.generate(n, dist, seed=ranks.rank)
+    A = torch.empty_like(inp)
+    B = torch.empty_like(inp)
+    ws = lsb.alloc_workspace(n, bits)
+    stream = torch.cuda.current_stream()
+
+    def one_sort():
+        A.copy_(inp)  # restore the unsorted input (not timed)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        lsb.sort_pairs(A, B, bits, workspace=ws)
+        e1.record(stream)
+        return e0, e1
+
+    for _ in range(max(args.warmup, 0)):
+        one_sort()
+    torch.cuda.synchronize()
+    st = lsb.query(ws)
+    if st.device_status != 0:
+        raise RuntimeError(f"device status {st.device_status} after warm-up")
+    bad = lsb.verify(inp, A)
+    if bad:
+        raise RuntimeError(f"warm-up sort differs from the stable sort ({bad} violations)")
+    passes_run = st.passes_run
+
+    # timed region
+    clocks = ClockSampler(torch.cuda.current_device())
+    ranks.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    time.sleep(0.3)  # let the sampler start
+    events = [one_sort() for _ in range(args.steps)]
+    torch.cuda.synchronize()
+    ranks.barrier()
+    clk = clocks.stop()
+    step_ms = [a.elapsed_time(b) for a, b in events]
+    local_s = sum(step_ms) / 1e3
+    t = ranks.max(local_s)
+    value = n * ranks.world * args.steps / t / 1e6
+    bad = lsb.verify(inp, A)
+    if bad:
+        raise RuntimeError(f"timed sort differs from the stable sort ({bad} violations)")
+
+    # per-kernel device times (separate, profiled steps; same work)
+    lsb.profile_read()
+    lsb.profile_enable(True)
+    prof_steps = min(args.steps, 5)
+    for _ in range(prof_steps):
+        one_sort()
+    torch.cuda.synchronize()
+    lsb.profile_enable(False)
+    prof = lsb.profile_read()
+    kernels = {k: {"launches_per_step": v[0] / prof_steps, "mean_ms": v[1] / v[0]} for k, v in prof.items()}
+    launches_per_step = sum(v[0] for v in prof.values()) / prof_steps
+    dom = max(prof.items(), key=lambda kv: kv[1][1])[0]
+    dom_ms = prof[dom][1] / prof[dom][0]
+    # algorithmic bytes per launch of the dominant kernel (per element, x n)
+    per_elem = {"task_scatter": 32, "onesweep_scatter": 32, "task_count": 8, "hist_digits": 8,
+                "final_copy": 32}.get(dom, 0)
+    peaks = measured_peaks()
+    achieved = per_elem * n / (dom_ms / 1e3) / 1e9
+    traffic, traffic_src = committed_traffic(dom, n, bits)
+    ms_per_step = t * 1e3 / args.steps
+    sort_bytes = algorithmic_bytes_per_element(bits, passes_run) * n
+    out = {
+        "metric": METRIC,
+        "value": round(value, 3),
+        "unit": UNIT,
+        "n_gpus": ranks.world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(ms_per_step, 4),
+        "p50_ms": round(statistics.median(step_ms), 4),
+        "p99_ms": round(sorted(step_ms)[min(len(step_ms) - 1, int(0.99 * len(step_ms)))], 4),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "u64",
+        "data": "synthetic",
+        "config": {"workload": f"lsd-sort 2^{n.bit_length() - 1} {args.dist} u64 keys + u64 index values, "
+                               f"{bits}-bit digits ({passes_run} passes)",
+                   "n": n, "digit_bits": bits, "dist": args.dist, "parallelism": f"replicas x{ranks.world}",
+                   "l2": "inputs (16 B x n) far larger than L2; input restored by a 16 B x n copy before each step"},
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peaks["hbm_gbs"],
+                     "unit": "GB/s", "frac": round(achieved / peaks["hbm_gbs"], 4),
+                     "traffic": traffic, "traffic_source": traffic_src,
+                     "algorithmic_bytes_per_launch": per_elem * n, "mean_launch_ms": round(dom_ms, 4),
+                     "peak_source": peaks["source"]},
+        "sort_roofline": {"algorithmic_bytes_per_element": algorithmic_bytes_per_element(bits, passes_run),
+                          "achieved_gbs": round(sort_bytes / (ms_per_step / 1e3) / 1e9, 1),
+                          "frac": round(sort_bytes / (ms_per_step / 1e3) / 1e9 / peaks["hbm_gbs"], 4)},
+        "kernels": {k: {kk: round(vv, 4) for kk, vv in v.items()} for k, v in kernels.items()},
+        "gpu_launches": int(round(launches_per_step * args.steps)),
+        "clocks": clk,
+    }
+
+    # side measurement: the 8-bit-digit configuration of the same input
+    if not args.no_extra and bits != 8:
+        ws8 = lsb.alloc_workspace(n, 8)
+        ev = []
+        for i in range(2 + 3):
+            A.copy_(inp)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            lsb.sort_pairs(A, B, 8, workspace=ws8)
+            e1.record(stream)
+            if i >= 2:
+                ev.append((e0, e1))
+        torch.cuda.synchronize()
+        ms8 = statistics.mean(a.elapsed_time(b) for a, b in ev)
+        out["digit_bits_8"] = {"ms_per_step": round(ms8, 4), "value": round(n / (ms8 / 1e3) / 1e6, 3),
+                               "verify_violations": lsb.verify(inp, A)}
+        del ws8
+
+    # e2e through the host-buffer entry point
+    if not args.no_e2e:
+        del A, B, ws
+        torch.cuda.empty_cache()
+        h = torch.empty((n, 2), dtype=torch.int64, pin_memory=True)
+        times = []
+        for i in range(1 + args.e2e_steps):
+            h.copy_(inp)  # restore the unsorted input in host memory (not timed)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            lsb.sort_pairs_host(h, bits)
+            dt = time.perf_counter() - t0
+            if i >= 1:
+                times.append(dt)
+        te = ranks.max(sum(times))
+        ok = bool((h[1:, 0].cpu() >= h[:-1, 0].cpu()).all().item()) if n < (1 << 27) else None
+        out["e2e"] = {"value": round(n * ranks.world * len(times) / te / 1e6, 3), "unit": UNIT,
+                      "h2d_bytes_per_step": 16 * n, "d2h_bytes_per_step": 16 * n,
+                      "steps": len(times), "ms_per_step": round(te * 1e3 / len(times), 3),
+                      "call": "lsb_sort_pairs_host (pinned host buffer)", "sorted_check": ok}
+        del h
+
+    if ranks.rank == 0 and ranks.world == 1 and not args.no_cpu:
+        val, times, threads = cpu_sort_rate(args.cpu_sample, 3, warmup=1, budget_s=30.0)
+        out["cpu_baseline"] = {"value": round(val, 3), "unit": UNIT, "cores": threads, "kind": "port",
+                               "sample": f"{args.cpu_sample} uniform elements, 16-bit digits, "
+                                         f"{len(times)} timed sorts, {threads} simulated ranks"}
+    return out
+
+
+def main(argv=None):
+    args = args_parse(argv)
+    ranks = Ranks()
+    try:
+        out = cpu_arm(args, ranks) if args.impl == "reference" else gpu_arm(args, ranks)
+        if ranks.rank == 0 and out is not None:
+            print(json.dumps(out), flush=True)
+    finally:
+        ranks.close()
+
+
+if __name__ == "__main__":
+    main()

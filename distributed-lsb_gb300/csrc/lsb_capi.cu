@@ -1,0 +1,537 @@
+// lsb_capi.cu -- the C ABI of liblsb.so (declared in include/lsb.h).
+//
+// Host-side validation, workspace layout, the library-owned stream-ordered
+// memory pool, and the harness kernels (seeded input generation and the O(n)
+// device verifier). The pass kernels live in lsb_onesweep.cu and lsb_task.cu.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <mutex>
+#include <vector>
+
+#include "../../include/lsb.h"
+#include "lsb_internal.h"
+
+namespace lsb {
+
+static_assert(sizeof(lsb_elem_t) == sizeof(Elem), "ABI element matches the device element");
+
+// ---------------------------------------------------------------------------
+// device info and the library's memory pool
+
+struct PerDevice {
+  bool init = false;
+  DeviceInfo info;
+  cudaMemPool_t pool = nullptr;
+  uint64_t* zipf = nullptr;  // 2^20 Zipf thresholds, built on first use
+};
+static std::mutex g_mu;
+static std::vector<PerDevice> g_dev;
+
+static PerDevice* per_device() {
+  int dev = -1;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0) return nullptr;
+  std::lock_guard<std::mutex> lk(g_mu);
+  if ((int)g_dev.size() <= dev) g_dev.resize(dev + 1);
+  PerDevice& p = g_dev[dev];
+  if (!p.init) {
+    cudaDeviceProp prop;
+    if (cudaGetDeviceProperties(&prop, dev) != cudaSuccess) return nullptr;
+    p.info.device = dev;
+    p.info.sm_count = prop.multiProcessorCount;
+    p.info.max_smem_optin = (int)prop.sharedMemPerBlockOptin;
+    cudaMemPoolProps pp;
+    std::memset(&pp, 0, sizeof pp);
+    pp.allocType = cudaMemAllocationTypePinned;
+    pp.handleTypes = cudaMemHandleTypeNone;
+    pp.location.type = cudaMemLocationTypeDevice;
+    pp.location.id = dev;
+    if (cudaMemPoolCreate(&p.pool, &pp) != cudaSuccess) return nullptr;
+    uint64_t keep = UINT64_MAX;  // keep freed blocks for reuse by later calls
+    cudaMemPoolSetAttribute(p.pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    p.init = true;
+  }
+  return &p;
+}
+
+int current_device_info(DeviceInfo* info) {
+  PerDevice* p = per_device();
+  if (!p) return LSB_ERR_NO_DEVICE;
+  *info = p->info;
+  return 0;
+}
+
+static int pool_alloc(void** ptr, size_t bytes, cudaStream_t st) {
+  PerDevice* p = per_device();
+  if (!p) return LSB_ERR_NO_DEVICE;
+  if (bytes == 0) bytes = 256;
+  if (cudaMallocFromPoolAsync(ptr, bytes, p->pool, st) != cudaSuccess) {
+    cudaGetLastError();
+    return LSB_ERR_NO_MEMORY;
+  }
+  return 0;
+}
+
+// ---------------------------------------------------------------------------
+// workspace layout
+
+int plan_layout(int64_t n, int bits, int num_digits, Layout* L) {
+  DeviceInfo dev;
+  if (int rc = current_device_info(&dev)) return rc;
+  *L = Layout();
+  L->bits = bits;
+  L->num_digits = num_digits;
+  L->n = (uint32_t)n;
+  const size_t nbins = (size_t)1 << bits;
+  size_t off = kCtrlBytes;
+  if (bits <= 11) {
+    L->family = Family::kOnesweep;
+    L->tile_elems = onesweep_tile_elems(bits);
+    L->grid = onesweep_grid(bits, dev, L->n);
+    const uint32_t tiles = (uint32_t)((n + L->tile_elems - 1) / L->tile_elems);
+    L->ring_tiles = std::max<uint32_t>(1u, std::min<uint32_t>(tiles, 4u * L->grid + 64u));
+    L->off_hist = off;
+    off = align_up(off + (size_t)num_digits * nbins * 4u, 256);
+    L->off_gstart = off;
+    off = align_up(off + (size_t)num_digits * nbins * 4u, 256);
+    L->off_ring = off;
+    off = align_up(off + (size_t)L->ring_tiles * nbins * 8u, 256);
+    L->off_done = off;
+    off = align_up(off + (size_t)L->ring_tiles * 4u, 256);
+  } else {
+    L->family = Family::kTask;
+    L->tasks = task_count(dev, L->n);
+    L->off_table = off;
+    off = align_up(off + (size_t)L->tasks * nbins * 4u, 256);
+    L->off_totals = off;
+    off = align_up(off + nbins * 4u, 256);
+    L->off_dstart = off;
+    off = align_up(off + nbins * 4u, 256);
+  }
+  L->total = off;
+  return 0;
+}
+
+int run_passes(Elem* X, Elem* Y, int first_digit, int target_parity, void* ws, const Layout& L,
+               cudaStream_t st) {
+  unsigned char* w = static_cast<unsigned char*>(ws);
+  if (cudaMemsetAsync(w, 0, kCtrlBytes, st) != cudaSuccess) return LSB_ERR_CUDA;
+  int rc = (L.family == Family::kOnesweep) ? onesweep_run(X, Y, first_digit, target_parity, w, L, st)
+                                            : task_run(X, Y, first_digit, target_parity, w, L, st);
+  if (rc) return rc == 1 ? LSB_ERR_INVALID_ARG : LSB_ERR_CUDA;
+  return LSB_OK;
+}
+
+// ---------------------------------------------------------------------------
+// harness kernels
+
+__device__ __forceinline__ uint64_t splitmix64_at(uint64_t seed, uint64_t i) {
+  uint64_t z = seed + (i + 1u) * 0x9E3779B97F4A7C15ull;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+
+constexpr int kZipfKeys = 1 << 20;
+constexpr double kZipfS = 1.1;
+constexpr uint64_t kZipfKeyStream = 0x243F6A8885A308D3ull;
+constexpr uint64_t kZipfDrawStream = 0x13198A2E03707344ull;
+
+__global__ void k_generate(Elem* out, uint32_t n, int dist, uint64_t seed,
+                           const uint64_t* __restrict__ zipf) {
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (uint64_t)gridDim.x * blockDim.x) {
+    uint64_t k;
+    switch (dist) {
+      case LSB_DIST_UNIFORM: k = splitmix64_at(seed, i); break;
+      case LSB_DIST_LOW32: k = splitmix64_at(seed, i) & 0xFFFFFFFFull; break;
+      case LSB_DIST_ZIPF: {
+        const uint64_t u = splitmix64_at(seed + kZipfDrawStream, i);
+        uint32_t lo = 0, hi = kZipfKeys - 1;
+        while (lo < hi) {
+          const uint32_t mid = lo + (hi - lo) / 2;
+          if (u < zipf[mid]) hi = mid; else lo = mid + 1;
+        }
+        k = splitmix64_at(seed + kZipfKeyStream, lo);
+        break;
+      }
+      case LSB_DIST_EQUAL: k = splitmix64_at(seed, 0); break;
+      default: k = i ^ (i >> 3); break;  // LSB_DIST_NEARLY_SORTED
+    }
+    store_elem(out + i, Elem{k, i});
+  }
+}
+
+static int zipf_table(uint64_t** out, cudaStream_t st) {
+  PerDevice* p = per_device();
+  if (!p) return LSB_ERR_NO_DEVICE;
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (!p->zipf) {
+    // P(rank <= r) of Zipf(s) over kZipfKeys ranks, as 64-bit fixed point
+    std::vector<uint64_t> thr(kZipfKeys);
+    double h = 0.0;
+    for (int r = 0; r < kZipfKeys; r++) h += std::pow((double)(r + 1), -kZipfS);
+    double c = 0.0;
+    for (int r = 0; r < kZipfKeys; r++) {
+      c += std::pow((double)(r + 1), -kZipfS) / h;
+      const double t = c * 18446744073709551616.0;
+      thr[r] = (t >= 18446744073709551615.0) ? UINT64_MAX : (uint64_t)t;
+    }
+    thr[kZipfKeys - 1] = UINT64_MAX;
+    uint64_t* d = nullptr;
+    if (cudaMalloc(&d, sizeof(uint64_t) * kZipfKeys) != cudaSuccess) return LSB_ERR_NO_MEMORY;
+    if (cudaMemcpyAsync(d, thr.data(), sizeof(uint64_t) * kZipfKeys, cudaMemcpyHostToDevice, st) !=
+            cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess) {
+      cudaFree(d);
+      return LSB_ERR_CUDA;
+    }
+    p->zipf = d;
+  }
+  *out = p->zipf;
+  return 0;
+}
+
+__global__ void k_verify(const Elem* __restrict__ in, const Elem* __restrict__ out, uint32_t n,
+                         uint32_t* __restrict__ seen, unsigned long long* __restrict__ bad) {
+  unsigned long long local = 0;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (uint64_t)gridDim.x * blockDim.x) {
+    const Elem o = out[i];
+    if (i + 1 < n) {
+      const Elem q = out[i + 1];
+      if (o.key > q.key || (o.key == q.key && o.val >= q.val)) local++;  // order + stability
+    }
+    if (o.val >= n) {
+      local++;
+    } else {
+      const Elem s = in[o.val];
+      if (s.key != o.key || s.val != o.val) local++;  // element exists in the input
+      const uint32_t bit = 1u << (o.val & 31u);
+      if (atomicOr(seen + (o.val >> 5), bit) & bit) local++;  // each index once
+    }
+  }
+  if (local) atomicAdd(bad, local);
+}
+
+static int launch_grid(uint32_t n, int* grid) {
+  DeviceInfo dev;
+  if (int rc = current_device_info(&dev)) return rc;
+  *grid = (int)std::max<uint32_t>(1, std::min<uint32_t>((n + 255) / 256, dev.sm_count * 16u));
+  return 0;
+}
+
+// ---------------------------------------------------------------------------
+// profiling records
+
+struct ProfRec {
+  const char* name;
+  cudaEvent_t a, b;
+};
+static std::mutex g_prof_mu;
+static bool g_prof_on = false;
+static std::vector<ProfRec> g_prof;
+
+ProfScope::ProfScope(const char* name, cudaStream_t st) : name_(name), st_(st) {
+  bool on;
+  {
+    std::lock_guard<std::mutex> lk(g_prof_mu);
+    on = g_prof_on;
+  }
+  if (on && cudaEventCreate(&a_) == cudaSuccess) cudaEventRecord(a_, st_);
+  else a_ = nullptr;
+}
+
+ProfScope::~ProfScope() {
+  if (!a_) return;
+  cudaEvent_t b = nullptr;
+  if (cudaEventCreate(&b) != cudaSuccess) {
+    cudaEventDestroy(a_);
+    return;
+  }
+  cudaEventRecord(b, st_);
+  std::lock_guard<std::mutex> lk(g_prof_mu);
+  g_prof.push_back(ProfRec{name_, a_, b});
+}
+
+__global__ void k_u32_to_i64(const uint32_t* in, int64_t* out, uint32_t count) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < count) out[i] = (int64_t)in[i];
+}
+
+}  // namespace lsb
+
+// ---------------------------------------------------------------------------
+// validation helpers
+
+using namespace lsb;
+
+static bool aligned16(const void* p) { return ((uintptr_t)p & 15u) == 0; }
+static bool overlap(const void* a, const void* b, int64_t n) {
+  const uintptr_t x = (uintptr_t)a, y = (uintptr_t)b, len = (uintptr_t)n * 16u;
+  return x < y + len && y < x + len;
+}
+static int check_common(const void* a, const void* b, int64_t n, int bits) {
+  if (bits < 1 || bits > 16) return LSB_ERR_INVALID_ARG;
+  if (n < 0) return LSB_ERR_INVALID_ARG;
+  if (n > LSB_MAX_ELEMENTS) return LSB_ERR_TOO_LARGE;
+  if (n > 0 && (!a || !b)) return LSB_ERR_INVALID_ARG;
+  if (n > 0 && (!aligned16(a) || !aligned16(b))) return LSB_ERR_ALIGNMENT;
+  if (n > 0 && overlap(a, b, n)) return LSB_ERR_OVERLAP;
+  return LSB_OK;
+}
+
+extern "C" {
+
+const char* lsb_status_string(int s) {
+  switch (s) {
+    case LSB_OK: return "LSB_OK";
+    case LSB_ERR_INVALID_ARG: return "LSB_ERR_INVALID_ARG";
+    case LSB_ERR_ALIGNMENT: return "LSB_ERR_ALIGNMENT";
+    case LSB_ERR_TOO_LARGE: return "LSB_ERR_TOO_LARGE";
+    case LSB_ERR_WORKSPACE: return "LSB_ERR_WORKSPACE";
+    case LSB_ERR_CUDA: return "LSB_ERR_CUDA";
+    case LSB_ERR_DEVICE_TIMEOUT: return "LSB_ERR_DEVICE_TIMEOUT";
+    case LSB_ERR_NO_DEVICE: return "LSB_ERR_NO_DEVICE";
+    case LSB_ERR_OVERLAP: return "LSB_ERR_OVERLAP";
+    case LSB_ERR_NO_MEMORY: return "LSB_ERR_NO_MEMORY";
+    default: return "LSB_ERR_UNKNOWN";
+  }
+}
+
+int lsb_version(void) { return LSB_ABI_VERSION; }
+
+int lsb_num_passes(int digit_bits) {
+  if (digit_bits < 1 || digit_bits > 16) return -1;
+  return (64 + digit_bits - 1) / digit_bits;
+}
+
+int lsb_workspace_bytes(int64_t n, int digit_bits, size_t* bytes) {
+  if (!bytes || digit_bits < 1 || digit_bits > 16 || n < 0) return LSB_ERR_INVALID_ARG;
+  if (n > LSB_MAX_ELEMENTS) return LSB_ERR_TOO_LARGE;
+  Layout L;
+  if (int rc = plan_layout(n, digit_bits, lsb_num_passes(digit_bits), &L)) return rc;
+  *bytes = L.total;
+  return LSB_OK;
+}
+
+static int sort_or_pass(Elem* X, Elem* Y, int64_t n, int bits, int first_digit, int num_digits,
+                        int target_parity, void* ws, size_t ws_bytes, cudaStream_t st) {
+  Layout L;
+  if (int rc = plan_layout(n, bits, num_digits, &L)) return rc;
+  if (ws) {
+    if (((uintptr_t)ws & 255u) != 0 || ws_bytes < L.total) return LSB_ERR_WORKSPACE;
+    return run_passes(X, Y, first_digit, target_parity, ws, L, st);
+  }
+  if (ws_bytes != 0) return LSB_ERR_WORKSPACE;
+  void* w = nullptr;
+  if (int rc = pool_alloc(&w, L.total, st)) return rc;
+  int rc = run_passes(X, Y, first_digit, target_parity, w, L, st);
+  uint32_t dev_err = 0;
+  if (rc == LSB_OK &&
+      cudaMemcpyAsync(&dev_err, w, sizeof(uint32_t), cudaMemcpyDeviceToHost, st) != cudaSuccess)
+    rc = LSB_ERR_CUDA;
+  cudaFreeAsync(w, st);
+  if (cudaStreamSynchronize(st) != cudaSuccess && rc == LSB_OK) rc = LSB_ERR_CUDA;
+  if (rc == LSB_OK && dev_err) rc = (int)dev_err;
+  return rc;
+}
+
+int lsb_sort_pairs(lsb_elem_t* d_a, lsb_elem_t* d_b, int64_t n, int digit_bits, void* d_workspace,
+                   size_t workspace_bytes, void* stream) {
+  if (int rc = check_common(d_a, d_b, n, digit_bits)) return rc;
+  cudaStream_t st = (cudaStream_t)stream;
+  if (n <= 1) {  // nothing to reorder; leave a clean status behind
+    if (d_workspace && cudaMemsetAsync(d_workspace, 0, kCtrlBytes, st) != cudaSuccess)
+      return LSB_ERR_CUDA;
+    return LSB_OK;
+  }
+  return sort_or_pass(reinterpret_cast<Elem*>(d_a), reinterpret_cast<Elem*>(d_b), n, digit_bits, 0,
+                      lsb_num_passes(digit_bits), 0, d_workspace, workspace_bytes, st);
+}
+
+int lsb_pass(const lsb_elem_t* d_src, lsb_elem_t* d_dst, int64_t n, int digit_bits, int digit,
+             void* d_workspace, size_t workspace_bytes, void* stream) {
+  if (int rc = check_common(d_src, d_dst, n, digit_bits)) return rc;
+  if (digit < 0 || digit >= lsb_num_passes(digit_bits)) return LSB_ERR_INVALID_ARG;
+  cudaStream_t st = (cudaStream_t)stream;
+  if (n == 0) {
+    if (d_workspace && cudaMemsetAsync(d_workspace, 0, kCtrlBytes, st) != cudaSuccess)
+      return LSB_ERR_CUDA;
+    return LSB_OK;
+  }
+  // X = src is only ever read: one pass reads X and writes Y, or, when the
+  // digit is constant, the final copy moves X into Y.
+  return sort_or_pass(const_cast<Elem*>(reinterpret_cast<const Elem*>(d_src)),
+                      reinterpret_cast<Elem*>(d_dst), n, digit_bits, digit, 1, 1, d_workspace,
+                      workspace_bytes, st);
+}
+
+int lsb_histogram(const lsb_elem_t* d_data, int64_t n, int digit_bits, int64_t* d_counts,
+                  void* stream) {
+  if (digit_bits < 1 || digit_bits > 16 || n < 0 || !d_counts) return LSB_ERR_INVALID_ARG;
+  if (n > LSB_MAX_ELEMENTS) return LSB_ERR_TOO_LARGE;
+  if (n > 0 && !d_data) return LSB_ERR_INVALID_ARG;
+  if ((n > 0 && !aligned16(d_data)) || ((uintptr_t)d_counts & 7u)) return LSB_ERR_ALIGNMENT;
+  cudaStream_t st = (cudaStream_t)stream;
+  const Elem* data = reinterpret_cast<const Elem*>(d_data);
+  const int P = lsb_num_passes(digit_bits);
+  const uint32_t nbins = 1u << digit_bits;
+  DeviceInfo dev;
+  if (int rc = current_device_info(&dev)) return rc;
+  const size_t smem = (size_t)P * nbins * 4u;
+  if (smem <= (size_t)dev.max_smem_optin && digit_bits <= 11) {
+    void* tmp = nullptr;
+    if (int rc = pool_alloc(&tmp, smem, st)) return rc;
+    int rc = histogram_u32(data, (uint32_t)n, digit_bits, 0, P, (uint32_t*)tmp, st);
+    if (rc == 0) {
+      const uint32_t cnt = P * nbins;
+      k_u32_to_i64<<<(cnt + 255) / 256, 256, 0, st>>>((uint32_t*)tmp, d_counts, cnt);
+      if (cudaPeekAtLastError() != cudaSuccess) rc = LSB_ERR_CUDA;
+    } else {
+      rc = LSB_ERR_CUDA;
+    }
+    cudaFreeAsync(tmp, st);
+    return rc;
+  }
+  const uint32_t tasks = task_count(dev, (uint32_t)n);
+  void* table = nullptr;
+  if (int rc = pool_alloc(&table, (size_t)tasks * nbins * 4u, st)) return rc;
+  int rc = LSB_OK;
+  for (int p = 0; p < P && rc == LSB_OK; p++)
+    if (histogram_one_digit_i64(data, (uint32_t)n, digit_bits, p, (uint32_t*)table, tasks,
+                                d_counts + (size_t)p * nbins, st))
+      rc = LSB_ERR_CUDA;
+  cudaFreeAsync(table, st);
+  return rc;
+}
+
+int lsb_query(const void* d_workspace, void* stream, lsb_stats_t* stats) {
+  if (!d_workspace || !stats) return LSB_ERR_INVALID_ARG;
+  Ctrl c;
+  cudaStream_t st = (cudaStream_t)stream;
+  if (cudaMemcpyAsync(&c, d_workspace, sizeof c, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+      cudaStreamSynchronize(st) != cudaSuccess)
+    return LSB_ERR_CUDA;
+  std::memset(stats, 0, sizeof *stats);
+  stats->device_status = (int32_t)c.error;
+  stats->passes_planned = (int32_t)c.num_passes;
+  stats->passes_run = (int32_t)c.passes_run;
+  stats->skipped_mask = c.skip_mask_lo;
+  stats->final_copy = (int32_t)c.final_copy;
+  return stats->device_status;
+}
+
+int lsb_sort_pairs_host(lsb_elem_t* h_a, int64_t n, int digit_bits, void* stream) {
+  if (digit_bits < 1 || digit_bits > 16 || n < 0 || (n > 0 && !h_a)) return LSB_ERR_INVALID_ARG;
+  if (n > LSB_MAX_ELEMENTS) return LSB_ERR_TOO_LARGE;
+  if (n <= 1) return LSB_OK;
+  cudaStream_t st = (cudaStream_t)stream;
+  Layout L;
+  if (int rc = plan_layout(n, digit_bits, lsb_num_passes(digit_bits), &L)) return rc;
+  const size_t bytes = (size_t)n * sizeof(Elem);
+  void* buf = nullptr;
+  if (int rc = pool_alloc(&buf, 2 * bytes + L.total + 256, st)) return rc;
+  Elem* A = static_cast<Elem*>(buf);
+  Elem* B = A + n;
+  void* ws = (void*)align_up((uintptr_t)(B + n), 256);
+  int rc = LSB_OK;
+  if (cudaMemcpyAsync(A, h_a, bytes, cudaMemcpyHostToDevice, st) != cudaSuccess) rc = LSB_ERR_CUDA;
+  if (rc == LSB_OK) rc = run_passes(A, B, 0, 0, ws, L, st);
+  uint32_t dev_err = 0;
+  if (rc == LSB_OK &&
+      (cudaMemcpyAsync(h_a, A, bytes, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+       cudaMemcpyAsync(&dev_err, ws, sizeof dev_err, cudaMemcpyDeviceToHost, st) != cudaSuccess))
+    rc = LSB_ERR_CUDA;
+  cudaFreeAsync(buf, st);
+  if (cudaStreamSynchronize(st) != cudaSuccess && rc == LSB_OK) rc = LSB_ERR_CUDA;
+  if (rc == LSB_OK && dev_err) rc = (int)dev_err;
+  return rc;
+}
+
+int lsb_generate(lsb_elem_t* d_out, int64_t n, int dist, uint64_t seed, void* stream) {
+  if (n < 0 || (n > 0 && !d_out) || dist < 0 || dist > LSB_DIST_NEARLY_SORTED)
+    return LSB_ERR_INVALID_ARG;
+  if (n > LSB_MAX_ELEMENTS) return LSB_ERR_TOO_LARGE;
+  if (n > 0 && !aligned16(d_out)) return LSB_ERR_ALIGNMENT;
+  if (n == 0) return LSB_OK;
+  cudaStream_t st = (cudaStream_t)stream;
+  uint64_t* zipf = nullptr;
+  if (dist == LSB_DIST_ZIPF)
+    if (int rc = zipf_table(&zipf, st)) return rc;
+  int grid = 0;
+  if (int rc = launch_grid((uint32_t)n, &grid)) return rc;
+  k_generate<<<grid, 256, 0, st>>>(reinterpret_cast<Elem*>(d_out), (uint32_t)n, dist, seed, zipf);
+  return cudaPeekAtLastError() == cudaSuccess ? LSB_OK : LSB_ERR_CUDA;
+}
+
+int lsb_verify(const lsb_elem_t* d_in, const lsb_elem_t* d_out, int64_t n, uint64_t* h_mismatches,
+               void* stream) {
+  if (!h_mismatches || n < 0 || (n > 0 && (!d_in || !d_out))) return LSB_ERR_INVALID_ARG;
+  if (n > LSB_MAX_ELEMENTS) return LSB_ERR_TOO_LARGE;
+  *h_mismatches = 0;
+  if (n == 0) return LSB_OK;
+  cudaStream_t st = (cudaStream_t)stream;
+  const size_t words = ((size_t)n + 31) / 32;
+  void* tmp = nullptr;
+  if (int rc = pool_alloc(&tmp, words * 4u + 256u, st)) return rc;
+  unsigned long long* bad = static_cast<unsigned long long*>(tmp);
+  uint32_t* seen = reinterpret_cast<uint32_t*>(static_cast<unsigned char*>(tmp) + 256);
+  int rc = LSB_OK;
+  int grid = 0;
+  if ((rc = launch_grid((uint32_t)n, &grid)) == LSB_OK) {
+    if (cudaMemsetAsync(tmp, 0, words * 4u + 256u, st) != cudaSuccess) rc = LSB_ERR_CUDA;
+    if (rc == LSB_OK) {
+      k_verify<<<grid, 256, 0, st>>>(reinterpret_cast<const Elem*>(d_in),
+                                     reinterpret_cast<const Elem*>(d_out), (uint32_t)n, seen, bad);
+      unsigned long long h = 0;
+      if (cudaPeekAtLastError() != cudaSuccess ||
+          cudaMemcpyAsync(&h, bad, sizeof h, cudaMemcpyDeviceToHost, st) != cudaSuccess)
+        rc = LSB_ERR_CUDA;
+      cudaFreeAsync(tmp, st);
+      if (cudaStreamSynchronize(st) != cudaSuccess && rc == LSB_OK) rc = LSB_ERR_CUDA;
+      *h_mismatches = h;
+      return rc;
+    }
+  }
+  cudaFreeAsync(tmp, st);
+  cudaStreamSynchronize(st);
+  return rc;
+}
+
+int lsb_profile_enable(int on) {
+  std::lock_guard<std::mutex> lk(g_prof_mu);
+  g_prof_on = on != 0;
+  return LSB_OK;
+}
+
+int lsb_profile_read(lsb_kernel_time_t* out, int capacity, int* count) {
+  if (!count || capacity < 0 || (capacity > 0 && !out)) return LSB_ERR_INVALID_ARG;
+  std::vector<ProfRec> recs;
+  {
+    std::lock_guard<std::mutex> lk(g_prof_mu);
+    recs.swap(g_prof);
+  }
+  int used = 0, rc = LSB_OK;
+  for (const ProfRec& r : recs) {
+    float ms = 0.f;
+    if (cudaEventSynchronize(r.b) != cudaSuccess || cudaEventElapsedTime(&ms, r.a, r.b) != cudaSuccess)
+      rc = LSB_ERR_CUDA;
+    cudaEventDestroy(r.a);
+    cudaEventDestroy(r.b);
+    int k = 0;
+    while (k < used && std::strncmp(out[k].name, r.name, sizeof(out[k].name)) != 0) k++;
+    if (k == used) {
+      if (used == capacity) continue;
+      std::memset(&out[k], 0, sizeof(out[k]));
+      std::strncpy(out[k].name, r.name, sizeof(out[k].name) - 1);
+      used++;
+    }
+    out[k].launches += 1;
+    out[k].total_ms += ms;
+  }
+  *count = used;
+  return rc;
+}
+
+}  // extern "C"

@@ -1,0 +1,148 @@
+// lsb_device.cuh -- device-side definitions shared by the pass kernels.
+//
+// The reference pass (mpi/mpi_lsbsort.cpp:493-589) runs on MPI ranks; here a
+// rank is a CTA. Its count exchange (copyCountsToGlobalCounts, :339-395),
+// global exclusive scan (exclusiveScan, :397-426) and start redistribution
+// (copyStartsFromGlobalStarts, :428-491) become on-device work driven by the
+// control block below, and its Alltoallv of 24-byte shuffle records (:575)
+// becomes direct 16-byte stores into the destination array in HBM.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace lsb {
+
+constexpr int kMaxPasses = 64;  // digit_bits = 1 gives 64 passes
+
+// Device status codes (same values as include/lsb.h).
+constexpr uint32_t kStatusOk = 0;
+constexpr uint32_t kStatusTimeout = 6;
+
+// Where a bounded wait ran out (ctrl->err_where), for diagnostics.
+constexpr uint32_t kWhereLookback = 1;
+constexpr uint32_t kWhereRingReuse = 2;
+
+// Spin limit for every device-side wait: after this many polls (with a
+// nanosleep back-off of up to 256 ns each) the kernel records
+// kStatusTimeout, skips its stores and returns, so no wait can hang the GPU.
+constexpr uint32_t kSpinLimit = 1u << 22;
+
+// Control block at the start of every workspace. Zeroed by
+// the host before each sort or pass; written only by the kernels after that.
+struct Ctrl {
+  uint32_t error;                  // kStatusOk or kStatusTimeout (first error wins)
+  uint32_t err_where;              // kWhere* of the first error
+  uint32_t skip_mask_lo;           // bit p: digit p constant, pass skipped (p < 32)
+  uint32_t skip_mask_hi;           // same for p in [32, 64)
+  uint32_t passes_run;             // passes actually executed
+  uint32_t final_copy;             // 1 if the result had to be copied back
+  uint32_t num_passes;             // planned passes
+  uint32_t pad0;
+  uint32_t parity[kMaxPasses + 1]; // parity[p]: 0 = pass p reads X, writes Y; 1 = reads Y, writes X
+  uint32_t ticket[kMaxPasses];     // tile dispenser per pass (in-order tile dispatch)
+};
+static_assert(sizeof(Ctrl) <= 1024, "control block must fit its 1 KiB slot");
+constexpr size_t kCtrlBytes = 1024;
+
+struct __align__(16) Elem {
+  uint64_t key;
+  uint64_t val;
+};
+static_assert(sizeof(Elem) == 16, "element is the reference's 16-byte SortElement");
+
+__device__ __forceinline__ uint32_t digit_of(uint64_t key, int shift, uint32_t mask) {
+  return (uint32_t)(key >> shift) & mask;  // getBucket, mpi/mpi_lsbsort.cpp:215-217
+}
+
+__device__ __forceinline__ Elem load_elem_stream(const Elem* p) {
+  // 16-byte read-only load that does not allocate in L1 (each element is read once).
+  ulonglong2 v;
+  asm volatile("ld.global.nc.L1::no_allocate.v2.u64 {%0, %1}, [%2];"
+               : "=l"(v.x), "=l"(v.y)
+               : "l"(p));
+  Elem e;
+  e.key = v.x;
+  e.val = v.y;
+  return e;
+}
+
+__device__ __forceinline__ void store_elem(Elem* p, const Elem& e) {
+  asm volatile("st.global.v2.u64 [%0], {%1, %2};" ::"l"(p), "l"(e.key), "l"(e.val) : "memory");
+}
+
+__device__ __forceinline__ uint64_t ld_relaxed_u64(const uint64_t* p) {
+  uint64_t v;
+  asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_relaxed_u64(uint64_t* p, uint64_t v) {
+  asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+__device__ __forceinline__ uint32_t ld_acquire_u32(const uint32_t* p) {
+  uint32_t v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release_u32(uint32_t* p, uint32_t v) {
+  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+__device__ __forceinline__ void record_error(Ctrl* ctrl, uint32_t code, uint32_t where) {
+  if (atomicCAS(&ctrl->error, 0u, code) == 0u) atomicExch(&ctrl->err_where, where);
+}
+
+__device__ __forceinline__ uint32_t lane_id() { return threadIdx.x & 31u; }
+__device__ __forceinline__ uint32_t lanemask_lt() {
+  uint32_t m;
+  asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+  return m;
+}
+
+// Look-back status word: [63:62] flag, [61:32] tag, [31:0] value.
+// The tag names (pass, tile) so that entries left by an earlier pass or tile
+// that shared the ring slot are never mistaken for the awaited one.
+constexpr uint64_t kFlagAgg = 1ull << 62;   // value = this tile's count of the digit
+constexpr uint64_t kFlagIncl = 2ull << 62;  // value = count in tiles [0, tile]
+__device__ __forceinline__ uint32_t ring_tag(int pass, uint32_t tile) {
+  return ((uint32_t)(pass + 1) << 24) | (tile & 0xFFFFFFu);
+}
+__device__ __forceinline__ uint64_t pack_status(uint64_t flag, uint32_t tag, uint32_t value) {
+  return flag | ((uint64_t)(tag & 0x3FFFFFFFu) << 32) | value;
+}
+__device__ __forceinline__ uint32_t status_tag(uint64_t s) { return (uint32_t)(s >> 32) & 0x3FFFFFFFu; }
+__device__ __forceinline__ uint64_t status_flag(uint64_t s) { return s & (3ull << 62); }
+
+// Exclusive block-wide scan of one uint32 per thread. `warp_tot` is a shared
+// array of 33 entries. Returns the exclusive prefix and
+// writes the block total to *total (all threads).
+__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* warp_tot,
+                                                         uint32_t* total) {
+  const uint32_t lane = lane_id(), warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  uint32_t x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= (uint32_t)o) x += y;
+  }
+  if (lane == 31) warp_tot[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    uint32_t t = lane < nwarps ? warp_tot[lane] : 0u;
+    uint32_t s = t;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      uint32_t y = __shfl_up_sync(0xffffffffu, s, o);
+      if (lane >= (uint32_t)o) s += y;
+    }
+    if (lane < nwarps) warp_tot[lane] = s - t;  // exclusive warp offsets
+    if (lane == nwarps - 1) warp_tot[32] = s;   // block total
+  }
+  __syncthreads();
+  uint32_t r = warp_tot[warp] + x - v;
+  *total = warp_tot[32];
+  __syncthreads();
+  return r;
+}
+
+}  // namespace lsb

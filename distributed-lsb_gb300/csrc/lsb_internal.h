@@ -1,0 +1,101 @@
+// lsb_internal.h -- host-side plumbing shared by the translation units of
+// liblsb.so: the workspace layout and the pass drivers of the two kernel
+// families.
+//
+//  * "onesweep" family (digit_bits <= 11): one upfront read of the keys builds
+//    the counts of every digit, then one stable scatter kernel per pass whose
+//    tiles resolve their global offsets by decoupled look-back.
+//  * "task" family (digit_bits >= 12, the reference's 16-bit digits): per pass
+//    a count kernel over contiguous tasks, a digit-major scan of the
+//    [digit][task] count table and a stable scatter -- the reference's own
+//    pass structure (localShuffle counts, GlobalCounts transpose, exclusive
+//    scan, shuffle) with MPI ranks replaced by CTAs.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "lsb_device.cuh"
+
+namespace lsb {
+
+struct DeviceInfo {
+  int device = -1;
+  int sm_count = 0;
+  int max_smem_optin = 0;
+};
+// Properties of the current device (cached per device id).
+int current_device_info(DeviceInfo* info);
+
+enum class Family { kOnesweep = 0, kTask = 1 };
+
+// Byte offsets inside the caller's workspace (all 256-byte aligned).
+struct Layout {
+  Family family = Family::kOnesweep;
+  int bits = 0;
+  int num_digits = 0;  // passes covered by this call
+  uint32_t n = 0;
+  size_t total = 0;
+  // onesweep family
+  size_t off_hist = 0;    // uint32 [num_digits][2^b]  digit counts
+  size_t off_gstart = 0;  // uint32 [num_digits][2^b]  exclusive digit starts
+  size_t off_ring = 0;    // uint64 [ring_tiles][2^b]  look-back status ring
+  size_t off_done = 0;    // uint32 [ring_tiles]       per-slot completion tags
+  uint32_t ring_tiles = 0;
+  uint32_t tile_elems = 0;
+  uint32_t grid = 0;      // persistent scatter CTAs
+  // task family
+  size_t off_table = 0;   // uint32 [tasks][2^b]  counts -> starts (cursors)
+  size_t off_totals = 0;  // uint32 [2^b]         digit totals
+  size_t off_dstart = 0;  // uint32 [2^b]         exclusive digit starts
+  uint32_t tasks = 0;
+};
+
+int plan_layout(int64_t n, int bits, int num_digits, Layout* out);
+
+// Runs passes [first_digit, first_digit + L.num_digits) over buffers X and Y.
+// Pass data starts in X. When target_parity is 0 the result ends in X (sort),
+// when 1 it ends in Y (single pass). Stream-ordered, no host synchronisation.
+int run_passes(Elem* X, Elem* Y, int first_digit, int target_parity, void* ws,
+               const Layout& L, cudaStream_t st);
+
+// Family drivers (lsb_onesweep.cu, lsb_task.cu).
+int onesweep_run(Elem* X, Elem* Y, int first_digit, int target_parity, unsigned char* ws,
+                 const Layout& L, cudaStream_t st);
+int task_run(Elem* X, Elem* Y, int first_digit, int target_parity, unsigned char* ws,
+             const Layout& L, cudaStream_t st);
+uint32_t onesweep_tile_elems(int bits);
+uint32_t onesweep_grid(int bits, const DeviceInfo& dev, uint32_t n);
+uint32_t task_count(const DeviceInfo& dev, uint32_t n);
+
+// All-digit histogram into uint32 counts (onesweep family sizes only:
+// num_digits * 2^b * 4 bytes of shared memory must fit).
+int histogram_u32(const Elem* data, uint32_t n, int bits, int first_digit, int num_digits,
+                  uint32_t* d_counts, cudaStream_t st);
+// One digit's counts for any b, via the task count kernel: d_table must hold
+// tasks * 2^b uint32; result summed into d_counts64[2^b].
+int histogram_one_digit_i64(const Elem* data, uint32_t n, int bits, int digit, uint32_t* d_table,
+                            uint32_t tasks, int64_t* d_counts64, cudaStream_t st);
+
+// Copies the pass data into the target buffer when an odd number of passes
+// left it in the other one (decided on the device from ctrl->parity).
+int final_copy(Elem* X, Elem* Y, uint32_t n, int num_digits, int target_parity, Ctrl* ctrl,
+               cudaStream_t st);
+
+inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+// Profiling scope: when lsb_profile_enable(1) is in effect, records a CUDA
+// event on `st` at construction and another at destruction, under `name`.
+class ProfScope {
+ public:
+  ProfScope(const char* name, cudaStream_t st);
+  ~ProfScope();
+
+ private:
+  const char* name_;
+  cudaStream_t st_;
+  cudaEvent_t a_ = nullptr;
+};
+
+}  // namespace lsb

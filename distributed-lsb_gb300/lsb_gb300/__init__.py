@@ -1,0 +1,218 @@
+"""Python host binding of liblsb.so, the GB300 LSD radix-sort pass library.
+
+The library's C ABI (include/lsb.h) is the drop-in boundary for the sort loop
+of mpi/mpi_lsbsort.cpp (mppf/distributed-lsb): ``sort_pairs`` is ``mySort``
+(mpi/mpi_lsbsort.cpp:592-597), ``global_shuffle`` is one ``globalShuffle``
+pass (:493-589) and ``histogram`` is the count loop of ``localShuffle``
+(:237-241) for every digit. This module only loads the shared library and
+passes device pointers through ctypes; PyTorch supplies device memory and
+streams. There is no fallback: if liblsb.so is missing or fails to load, every
+call raises.
+
+Arrays are int64 CUDA tensors of shape (n, 2) -- column 0 the key, column 1
+the value, bit-for-bit the reference's 16-byte ``SortElement``; view them as
+uint64 on the host (``t.cpu().numpy().view(numpy.uint64)``).
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+from ._build import LIB_PATH, build, lib_path  # noqa: F401
+
+LSB_OK = 0
+LSB_ERR_INVALID_ARG = 1
+LSB_ERR_ALIGNMENT = 2
+LSB_ERR_TOO_LARGE = 3
+LSB_ERR_WORKSPACE = 4
+LSB_ERR_CUDA = 5
+LSB_ERR_DEVICE_TIMEOUT = 6
+LSB_ERR_NO_DEVICE = 7
+LSB_ERR_OVERLAP = 8
+LSB_ERR_NO_MEMORY = 9
+
+DIST_UNIFORM, DIST_LOW32, DIST_ZIPF, DIST_EQUAL, DIST_NEARLY_SORTED = 0, 1, 2, 3, 4
+DIST_NAMES = {"uniform": 0, "low32": 1, "zipf": 2, "equal": 3, "nearly_sorted": 4}
+
+# Every symbol include/lsb.h declares, with its ctypes signature.
+_P = ctypes.c_void_p
+_I64 = ctypes.c_int64
+SIGNATURES = {
+    "lsb_status_string": (ctypes.c_char_p, [ctypes.c_int]),
+    "lsb_version": (ctypes.c_int, []),
+    "lsb_num_passes": (ctypes.c_int, [ctypes.c_int]),
+    "lsb_workspace_bytes": (ctypes.c_int, [_I64, ctypes.c_int, ctypes.POINTER(ctypes.c_size_t)]),
+    "lsb_sort_pairs": (ctypes.c_int, [_P, _P, _I64, ctypes.c_int, _P, ctypes.c_size_t, _P]),
+    "lsb_pass": (ctypes.c_int, [_P, _P, _I64, ctypes.c_int, ctypes.c_int, _P, ctypes.c_size_t, _P]),
+    "lsb_histogram": (ctypes.c_int, [_P, _I64, ctypes.c_int, _P, _P]),
+    "lsb_query": (ctypes.c_int, [_P, _P, _P]),
+    "lsb_sort_pairs_host": (ctypes.c_int, [_P, _I64, ctypes.c_int, _P]),
+    "lsb_generate": (ctypes.c_int, [_P, _I64, ctypes.c_int, ctypes.c_uint64, _P]),
+    "lsb_verify": (ctypes.c_int, [_P, _P, _I64, ctypes.POINTER(ctypes.c_uint64), _P]),
+    "lsb_profile_enable": (ctypes.c_int, [ctypes.c_int]),
+    "lsb_profile_read": (ctypes.c_int, [_P, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]),
+}
+
+
+class KernelTime(ctypes.Structure):
+    """lsb_kernel_time_t"""
+
+    _fields_ = [("name", ctypes.c_char * 40), ("launches", ctypes.c_int64), ("total_ms", ctypes.c_double)]
+
+
+class Stats(ctypes.Structure):
+    """lsb_stats_t"""
+
+    _fields_ = [
+        ("device_status", ctypes.c_int32),
+        ("passes_planned", ctypes.c_int32),
+        ("passes_run", ctypes.c_int32),
+        ("skipped_mask", ctypes.c_uint32),
+        ("final_copy", ctypes.c_int32),
+        ("digit_bits", ctypes.c_int32),
+        ("n", ctypes.c_int64),
+    ]
+
+
+class LsbError(RuntimeError):
+    def __init__(self, status: int, what: str):
+        self.status = status
+        super().__init__(f"{what}: {status_string(status)} ({status})")
+
+
+_lib = None
+
+
+def load(path: str | None = None):
+    """Load liblsb.so (once). Raises if it is missing: there is no fallback."""
+    global _lib
+    if _lib is None:
+        p = path or lib_path()
+        if not os.path.exists(p):
+            raise FileNotFoundError(f"liblsb.so not built ({p}); run build() first")
+        L = ctypes.CDLL(p)
+        for name, (res, args) in SIGNATURES.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def status_string(status: int) -> str:
+    try:
+        return load().lsb_status_string(status).decode()
+    except Exception:  # pragma: no cover - only for messages
+        return str(status)
+
+
+def _check(rc: int, what: str) -> None:
+    if rc != LSB_OK:
+        raise LsbError(rc, what)
+
+
+def _stream_ptr(stream):
+    if stream is None:
+        import torch
+
+        stream = torch.cuda.current_stream()
+    return ctypes.c_void_p(stream.cuda_stream)
+
+
+def _ptr(t) -> ctypes.c_void_p:
+    return ctypes.c_void_p(t.data_ptr()) if t is not None and t.numel() else ctypes.c_void_p(0)
+
+
+def num_passes(digit_bits: int) -> int:
+    return load().lsb_num_passes(digit_bits)
+
+
+def workspace_bytes(n: int, digit_bits: int) -> int:
+    out = ctypes.c_size_t(0)
+    _check(load().lsb_workspace_bytes(n, digit_bits, ctypes.byref(out)), "lsb_workspace_bytes")
+    return out.value
+
+
+def alloc_workspace(n: int, digit_bits: int, device=None):
+    import torch
+
+    nbytes = workspace_bytes(n, digit_bits)
+    return torch.empty(max(nbytes, 256), dtype=torch.uint8, device=device or "cuda")
+
+
+def sort_pairs(a, b, digit_bits: int = 16, workspace=None, stream=None) -> None:
+    """mySort(A, B): sorts ``a`` (int64 (n, 2) CUDA tensor) in place by key,
+    stably; ``b`` is scratch of the same shape. Asynchronous when a workspace
+    tensor is given, blocking (and status-checked) otherwise."""
+    n = a.shape[0]
+    ws = _ptr(workspace) if workspace is not None else ctypes.c_void_p(0)
+    wsb = workspace.numel() if workspace is not None else 0
+    _check(load().lsb_sort_pairs(_ptr(a), _ptr(b), n, digit_bits, ws, wsb, _stream_ptr(stream)),
+           "lsb_sort_pairs")
+
+
+def global_shuffle(src, dst, digit: int, digit_bits: int = 16, workspace=None, stream=None) -> None:
+    """One pass: ``dst`` = ``src`` stably sorted by ``digit``."""
+    n = src.shape[0]
+    ws = _ptr(workspace) if workspace is not None else ctypes.c_void_p(0)
+    wsb = workspace.numel() if workspace is not None else 0
+    _check(load().lsb_pass(_ptr(src), _ptr(dst), n, digit_bits, digit, ws, wsb, _stream_ptr(stream)),
+           "lsb_pass")
+
+
+def histogram(data, digit_bits: int = 16, stream=None):
+    """Counts of every digit of every pass: int64 CUDA tensor [passes, 2^b]."""
+    import torch
+
+    p = num_passes(digit_bits)
+    out = torch.empty((p, 1 << digit_bits), dtype=torch.int64, device=data.device)
+    _check(load().lsb_histogram(_ptr(data), data.shape[0], digit_bits, _ptr(out), _stream_ptr(stream)),
+           "lsb_histogram")
+    return out
+
+
+def query(workspace, stream=None) -> Stats:
+    s = Stats()
+    load().lsb_query(_ptr(workspace), _stream_ptr(stream), ctypes.byref(s))
+    return s
+
+
+def sort_pairs_host(array, digit_bits: int = 16) -> None:
+    """Host-memory mySort on a numpy uint64 (n, 2) array or a CPU tensor, in
+    place: copy in, sort, copy out (blocking)."""
+    if hasattr(array, "data_ptr"):
+        ptr, n = array.data_ptr(), array.shape[0]
+    else:
+        ptr, n = array.ctypes.data, array.shape[0]
+    _check(load().lsb_sort_pairs_host(ctypes.c_void_p(ptr), n, digit_bits, _stream_ptr(None)),
+           "lsb_sort_pairs_host")
+
+
+def generate(n: int, dist: int = DIST_UNIFORM, seed: int = 1, out=None, device=None, stream=None):
+    import torch
+
+    if out is None:
+        out = torch.empty((n, 2), dtype=torch.int64, device=device or "cuda")
+    _check(load().lsb_generate(_ptr(out), n, dist, seed, _stream_ptr(stream)), "lsb_generate")
+    return out
+
+
+def profile_enable(on: bool = True) -> None:
+    _check(load().lsb_profile_enable(1 if on else 0), "lsb_profile_enable")
+
+
+def profile_read() -> dict:
+    """{kernel name: (launches, total device ms)} since the last read."""
+    arr = (KernelTime * 64)()
+    cnt = ctypes.c_int(0)
+    _check(load().lsb_profile_read(ctypes.cast(arr, ctypes.c_void_p), 64, ctypes.byref(cnt)), "lsb_profile_read")
+    return {arr[i].name.decode(): (arr[i].launches, arr[i].total_ms) for i in range(cnt.value)}
+
+
+def verify(inp, out, stream=None) -> int:
+    """Number of violations of "out is the stable sort by key of inp"
+    (0 = identical to the reference's std::stable_sort check)."""
+    bad = ctypes.c_uint64(0)
+    _check(load().lsb_verify(_ptr(inp), _ptr(out), inp.shape[0], ctypes.byref(bad), _stream_ptr(stream)),
+           "lsb_verify")
+    return bad.value

@@ -1,0 +1,173 @@
+/*
+ * lsb.h -- C ABI of the GB300 LSD radix-sort pass library (liblsb.so).
+ *
+ * Drop-in boundary for the sort loop of mpi/mpi_lsbsort.cpp in
+ * mppf/distributed-lsb. The reference has no FFI of its own: its boundary is
+ * the C++ function `void mySort(DistributedArray<SortElement>& A,
+ * DistributedArray<SortElement>& B)` (mpi/mpi_lsbsort.cpp:592-597) and the
+ * per-digit pass `globalShuffle(A, B, digit)` (mpi/mpi_lsbsort.cpp:493-589).
+ * Each entry point below names the reference code it replaces.
+ *
+ * Conventions
+ *  - Element layout is the reference's SortElement (mpi/mpi_lsbsort.cpp:30-33):
+ *    16 bytes, key then value, both uint64; the key is sorted by, the value
+ *    is carried. Sorting is stable, so with value = original index the
+ *    result is unique and equals std::stable_sort by key.
+ *  - Device pointers are caller-owned, 16-byte aligned, and A and B must not
+ *    overlap. Host pointers (the *_host entry points) may be any memory.
+ *  - digit_bits b is in [1, 16]; the number of passes is ceil(64 / b), which is
+ *    the reference's N_DIGITS = 64/RADIX = 4 for its RADIX = 16
+ *    (mpi/mpi_lsbsort.cpp:22-23). Passes whose digit is the same for every
+ *    element are skipped: a stable sort by a constant digit is the identity.
+ *  - n is in [0, LSB_MAX_ELEMENTS].
+ *  - Every call returns LSB_OK or an LSB_ERR_* code; nothing aborts and no
+ *    C++ exception crosses the ABI (the reference aborts on MPI errors,
+ *    mpi/mpi_lsbsort.cpp:18-20).
+ *  - Calls taking a `stream` (a cudaStream_t, NULL = legacy default stream)
+ *    are stream-ordered and return before the GPU work finishes, unless the
+ *    comment says otherwise. Device-side failures (a bounded wait that ran
+ *    out) are recorded in the workspace and reported by lsb_query().
+ *    Concurrent calls on different streams need distinct workspaces.
+ */
+#ifndef LSB_H
+#define LSB_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define LSB_ABI_VERSION 1
+#define LSB_MAX_ELEMENTS ((int64_t)0xFFFFFFFF) /* positions are 32-bit on the device */
+
+typedef struct lsb_elem {
+  uint64_t key; /* to sort by   (SortElement::key) */
+  uint64_t val; /* carried along (SortElement::val) */
+} lsb_elem_t;
+
+enum lsb_status {
+  LSB_OK = 0,
+  LSB_ERR_INVALID_ARG = 1,    /* null pointer, n < 0, digit_bits or digit out of range */
+  LSB_ERR_ALIGNMENT = 2,      /* a device pointer is not 16-byte aligned               */
+  LSB_ERR_TOO_LARGE = 3,      /* n > LSB_MAX_ELEMENTS                                   */
+  LSB_ERR_WORKSPACE = 4,      /* workspace NULL with nonzero size, too small, unaligned */
+  LSB_ERR_CUDA = 5,           /* a CUDA runtime call failed                             */
+  LSB_ERR_DEVICE_TIMEOUT = 6, /* a bounded device-side wait ran out; output undefined  */
+  LSB_ERR_NO_DEVICE = 7,      /* no usable CUDA device                                  */
+  LSB_ERR_OVERLAP = 8,        /* A and B (or src and dst) overlap                       */
+  LSB_ERR_NO_MEMORY = 9       /* a library-managed allocation failed                    */
+};
+
+/* Input distributions for lsb_generate (the harness's seeded generators). */
+enum lsb_dist {
+  LSB_DIST_UNIFORM = 0,      /* key = splitmix64(seed, i)                          */
+  LSB_DIST_LOW32 = 1,        /* key = splitmix64(seed, i) & 0xffffffff              */
+  LSB_DIST_ZIPF = 2,         /* Zipf(1.1) ranks over 2^20 distinct uniform keys     */
+  LSB_DIST_EQUAL = 3,        /* every key equal                                    */
+  LSB_DIST_NEARLY_SORTED = 4 /* key = i ^ (i >> 3)                                  */
+};
+
+typedef struct lsb_stats {
+  int32_t device_status;  /* LSB_OK or LSB_ERR_DEVICE_TIMEOUT                      */
+  int32_t passes_planned; /* ceil(64 / digit_bits)                                  */
+  int32_t passes_run;     /* passes whose digit was not constant                    */
+  uint32_t skipped_mask;  /* bit p set: digit p was constant and its pass skipped   */
+  int32_t final_copy;     /* 1 if an odd pass count required a copy back into A     */
+  int32_t digit_bits;
+  int64_t n;
+} lsb_stats_t;
+
+/* Human-readable name of a status code (static string, never NULL). */
+const char* lsb_status_string(int status);
+
+/* LSB_ABI_VERSION of the loaded library. */
+int lsb_version(void);
+
+/* ceil(64 / digit_bits), or -1 if digit_bits is outside [1, 16].
+ * Replaces the compile-time N_DIGITS (mpi/mpi_lsbsort.cpp:23). */
+int lsb_num_passes(int digit_bits);
+
+/* Device workspace needed by lsb_sort_pairs / lsb_pass for (n, digit_bits), in
+ * bytes (the look-back ring, per-task count tables, pass plan and the device
+ * status word). It replaces the per-pass heap buffers of globalShuffle:
+ * counts/starts (mpi/mpi_lsbsort.cpp:501-502), GlobalCounts/GlobalStarts
+ * (:523-528) and the shuffle send/receive buffers (:550-555). */
+int lsb_workspace_bytes(int64_t n, int digit_bits, size_t* bytes);
+
+/* Stably sort d_a[0..n) by key; d_b[0..n) is scratch. Result in d_a.
+ * Replaces mySort(A, B) (mpi/mpi_lsbsort.cpp:592-597), whose result is also
+ * left in A with B as scratch (:591).
+ * d_workspace: a device buffer of at least lsb_workspace_bytes(n, b) bytes,
+ * 256-byte aligned, or NULL. With a workspace the call is asynchronous on
+ * `stream`; lsb_query() reports device-side failures. With NULL the library
+ * allocates stream-ordered scratch, waits for the sort to finish, frees it
+ * and returns the device status (blocking, like mySort). */
+int lsb_sort_pairs(lsb_elem_t* d_a, lsb_elem_t* d_b, int64_t n, int digit_bits,
+                   void* d_workspace, size_t workspace_bytes, void* stream);
+
+/* One pass: d_dst = d_src stably sorted by digit `digit` (bits
+ * [digit*b, digit*b + b) of the key). d_src is not modified.
+ * Replaces globalShuffle(A, B, digit) (mpi/mpi_lsbsort.cpp:493-589): the
+ * reference shuffles A into B locally and then places the result back in A;
+ * here source and destination are explicit, so a caller that wants the
+ * reference's in-place form swaps its two buffers after each pass.
+ * Workspace rules as for lsb_sort_pairs. */
+int lsb_pass(const lsb_elem_t* d_src, lsb_elem_t* d_dst, int64_t n, int digit_bits, int digit,
+             void* d_workspace, size_t workspace_bytes, void* stream);
+
+/* Per-digit counts of every pass from one read of the keys:
+ * d_counts[p * 2^b + d] (int64, lsb_num_passes(b) * 2^b entries, device memory)
+ * = number of elements whose digit p equals d. This is the count loop of
+ * localShuffle (mpi/mpi_lsbsort.cpp:237-241) for all digits at once, summed
+ * over ranks like GlobalCounts (mpi/mpi_lsbsort.cpp:339-395). Asynchronous. */
+int lsb_histogram(const lsb_elem_t* d_data, int64_t n, int digit_bits, int64_t* d_counts,
+                  void* stream);
+
+/* Waits for `stream`, then reads the pass plan and the device status word of
+ * the last sort or pass that used `d_workspace`. Returns stats->device_status. */
+int lsb_query(const void* d_workspace, void* stream, lsb_stats_t* stats);
+
+/* Host-memory form of mySort: copies h_a[0..n) to the device, sorts it with
+ * digit width b, and copies the result back into h_a (blocking). Device
+ * buffers are allocated and freed inside the call. This is the call a host
+ * program that keeps its arrays in host memory, like the reference
+ * (DistributedArray::localPart, mpi/mpi_lsbsort.cpp:105), makes. If h_a is
+ * page-locked the copies run at full link speed. */
+int lsb_sort_pairs_host(lsb_elem_t* h_a, int64_t n, int digit_bits, void* stream);
+
+/* Harness: fills d_out[0..n) with the seeded input of distribution `dist`;
+ * value = global index, like the reference's generator
+ * (mpi/mpi_lsbsort.cpp:686-692) with splitmix64 in place of pcg64. */
+int lsb_generate(lsb_elem_t* d_out, int64_t n, int dist, uint64_t seed, void* stream);
+
+/* Harness: O(n) device check that d_out is the stable sort by key of d_in,
+ * the reference's verification (mpi/mpi_lsbsort.cpp:755-784) without a host
+ * copy, assuming d_in[i].val == i (true for lsb_generate inputs). Checks
+ * sortedness of keys, strictly increasing values among equal keys, that
+ * every value is an index of d_in whose key matches, and that every index
+ * appears once. Blocking; *h_mismatches receives the number of violations
+ * (0 = identical to the reference's stable sort). Allocates n/8 bytes. */
+int lsb_verify(const lsb_elem_t* d_in, const lsb_elem_t* d_out, int64_t n, uint64_t* h_mismatches,
+               void* stream);
+
+/* Profiling (the reference only times mySort as a whole with steady_clock,
+ * mpi/mpi_lsbsort.cpp:731-745). When enabled, the library brackets each of
+ * its own kernel launches with CUDA events recorded on the launching stream;
+ * lsb_profile_read waits for those events and returns, per kernel, the number
+ * of launches and the summed device time since the previous read, then clears
+ * the records. Enabling it adds two event records per launch. */
+typedef struct lsb_kernel_time {
+  char name[40];    /* kernel name, NUL-terminated */
+  int64_t launches; /* launches recorded                        */
+  double total_ms;  /* summed time between each launch's events */
+} lsb_kernel_time_t;
+
+int lsb_profile_enable(int on);
+int lsb_profile_read(lsb_kernel_time_t* out, int capacity, int* count);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* LSB_H */

@@ -1,0 +1,52 @@
+"""Parity at the workload sizes: 2^24 against the reference's golden digest,
+and 2^28 / 2^30 through the O(n) device check (order + stability + every
+input index exactly once with its key = the reference's std::stable_sort)."""
+from __future__ import annotations
+
+import pytest
+
+from conftest import digest, to_dev, to_np
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("bits", [16, 11, 8])
+def test_2p24_uniform_matches_reference_golden(lsb, cuda, oracle, golden, bits):
+    c = [c for c in golden["cases"] if c["n"] == 1 << 24][0]
+    a = lsb.generate(c["n"], lsb.DIST_UNIFORM, c["seed"])
+    assert digest(to_np(a)) == c["input_sha256"]
+    b = cuda.empty_like(a)
+    ws = lsb.alloc_workspace(c["n"], bits)
+    lsb.sort_pairs(a, b, bits, workspace=ws)
+    assert lsb.query(ws).device_status == 0
+    assert digest(to_np(a)) == c["sorted_sha256"]
+
+
+def _sort_and_check(lsb, torch, n, dist, bits, seed=1):
+    inp = lsb.generate(n, dist, seed)
+    a = inp.clone()
+    b = torch.empty_like(a)
+    ws = lsb.alloc_workspace(n, bits)
+    lsb.sort_pairs(a, b, bits, workspace=ws)
+    st = lsb.query(ws)
+    assert st.device_status == 0
+    bad = lsb.verify(inp, a)
+    del inp, a, b, ws
+    torch.cuda.empty_cache()
+    return bad, st
+
+
+@pytest.mark.parametrize("dist,skipped16", [(1, 0b1100), (2, 0), (3, 0b1111), (4, 0b1100)])
+def test_2p28_skew_and_stability(lsb, cuda, dist, skipped16):
+    bad, st = _sort_and_check(lsb, cuda, 1 << 28, dist, 16)
+    assert bad == 0
+    assert st.skipped_mask == skipped16
+
+
+@pytest.mark.parametrize("bits", [16, 8])
+def test_2p30_uniform(lsb, cuda, bits):
+    free, _ = cuda.cuda.mem_get_info()
+    if free < 52 * 2**30:
+        pytest.skip("needs ~50 GB of free device memory")
+    bad, st = _sort_and_check(lsb, cuda, 1 << 30, lsb.DIST_UNIFORM, bits)
+    assert bad == 0 and st.passes_run == 64 // bits
