@@ -91,6 +91,9 @@ __device__ __forceinline__ void st_release_u32(uint32_t* p, uint32_t v) {
 __device__ __forceinline__ void record_error(Ctrl* ctrl, uint32_t code, uint32_t where) {
   if (atomicCAS(&ctrl->error, 0u, code) == 0u) atomicExch(&ctrl->err_where, where);
 }
+__device__ __forceinline__ bool error_raised(const Ctrl* ctrl) {
+  return *reinterpret_cast<const volatile uint32_t*>(&ctrl->error) != 0u;
+}
 
 __device__ __forceinline__ uint32_t lane_id() { return threadIdx.x & 31u; }
 __device__ __forceinline__ uint32_t lanemask_lt() {
@@ -104,8 +107,10 @@ __device__ __forceinline__ uint32_t lanemask_lt() {
 // that shared the ring slot are never mistaken for the awaited one.
 constexpr uint64_t kFlagAgg = 1ull << 62;   // value = this tile's count of the digit
 constexpr uint64_t kFlagIncl = 2ull << 62;  // value = count in tiles [0, tile]
+// tag = (pass + 1) in bits [29:23] (passes <= 64), tile in bits [22:0]
+// (tiles < 2^23, i.e. n < 2^35 at 4096-element tiles).
 __device__ __forceinline__ uint32_t ring_tag(int pass, uint32_t tile) {
-  return ((uint32_t)(pass + 1) << 24) | (tile & 0xFFFFFFu);
+  return ((uint32_t)(pass + 1) << 23) | (tile & 0x7FFFFFu);
 }
 __device__ __forceinline__ uint64_t pack_status(uint64_t flag, uint32_t tag, uint32_t value) {
   return flag | ((uint64_t)(tag & 0x3FFFFFFFu) << 32) | value;
