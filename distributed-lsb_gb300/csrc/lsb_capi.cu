@@ -40,18 +40,31 @@ static PerDevice* per_device() {
     p.info.device = dev;
     p.info.sm_count = prop.multiProcessorCount;
     p.info.max_smem_optin = (int)prop.sharedMemPerBlockOptin;
+    p.init = true;
+  }
+  return &p;
+}
+
+// The library's stream-ordered pool, created on the first allocation.
+static cudaMemPool_t device_pool() {
+  PerDevice* p = per_device();
+  if (!p) return nullptr;
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (!p->pool) {
     cudaMemPoolProps pp;
     std::memset(&pp, 0, sizeof pp);
     pp.allocType = cudaMemAllocationTypePinned;
     pp.handleTypes = cudaMemHandleTypeNone;
     pp.location.type = cudaMemLocationTypeDevice;
-    pp.location.id = dev;
-    if (cudaMemPoolCreate(&p.pool, &pp) != cudaSuccess) return nullptr;
+    pp.location.id = p->info.device;
+    if (cudaMemPoolCreate(&p->pool, &pp) != cudaSuccess) {
+      p->pool = nullptr;
+      return nullptr;
+    }
     uint64_t keep = UINT64_MAX;  // keep freed blocks for reuse by later calls
-    cudaMemPoolSetAttribute(p.pool, cudaMemPoolAttrReleaseThreshold, &keep);
-    p.init = true;
+    cudaMemPoolSetAttribute(p->pool, cudaMemPoolAttrReleaseThreshold, &keep);
   }
-  return &p;
+  return p->pool;
 }
 
 int current_device_info(DeviceInfo* info) {
@@ -62,10 +75,10 @@ int current_device_info(DeviceInfo* info) {
 }
 
 static int pool_alloc(void** ptr, size_t bytes, cudaStream_t st) {
-  PerDevice* p = per_device();
-  if (!p) return LSB_ERR_NO_DEVICE;
+  cudaMemPool_t pool = device_pool();
+  if (!pool) return LSB_ERR_NO_DEVICE;
   if (bytes == 0) bytes = 256;
-  if (cudaMallocFromPoolAsync(ptr, bytes, p->pool, st) != cudaSuccess) {
+  if (cudaMallocFromPoolAsync(ptr, bytes, pool, st) != cudaSuccess) {
     cudaGetLastError();
     return LSB_ERR_NO_MEMORY;
   }

@@ -49,6 +49,7 @@ SIGNATURES = {
     "lsb_sort_pairs_host": (ctypes.c_int, [_P, _I64, ctypes.c_int, _P]),
     "lsb_generate": (ctypes.c_int, [_P, _I64, ctypes.c_int, ctypes.c_uint64, _P]),
     "lsb_verify": (ctypes.c_int, [_P, _P, _I64, ctypes.POINTER(ctypes.c_uint64), _P]),
+    "lsb_sort_pairs_noalloc": (ctypes.c_int, [_P, _P, _I64, ctypes.c_int, _P]),
     "lsb_profile_enable": (ctypes.c_int, [ctypes.c_int]),
     "lsb_profile_read": (ctypes.c_int, [_P, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]),
 }

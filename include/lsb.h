@@ -152,6 +152,26 @@ int lsb_generate(lsb_elem_t* d_out, int64_t n, int dist, uint64_t seed, void* st
 int lsb_verify(const lsb_elem_t* d_in, const lsb_elem_t* d_out, int64_t n, uint64_t* h_mismatches,
                void* stream);
 
+/* Sort without any device allocation. No counterpart in the reference: it is
+ * for callers that may not allocate device memory -- a host framework that
+ * owns all GPU memory through its own arena, a latency-critical path that
+ * cannot take the device-wide synchronisation of cudaMalloc/cudaFree, code
+ * that must not fail half-way for lack of memory. It sorts d_a like
+ * lsb_sort_pairs (d_b scratch, result in d_a, same bytes) but takes its
+ * scratch from an 8 MiB array compiled into the library, which every GPU that
+ * loads the library holds until the process exits; it calls no allocator.
+ * Limits: digit_bits 1..8 (LSB_ERR_TOO_LARGE otherwise) and n up to
+ * LSB_MAX_ELEMENTS; if the scratch this GPU's kernel configuration needs is
+ * more than 8 MiB the call returns LSB_ERR_WORKSPACE before any GPU work.
+ * The first call on each device looks up the array's device address (with
+ * that device current); make that first call before any stream capture.
+ * All calls share the one array and it keeps the last call's contents (each
+ * call clears what must start at zero): calls whose GPU work overlaps, on
+ * different streams or host threads, race and corrupt each other's results.
+ * Blocking: waits for `stream` and returns the device status. */
+int lsb_sort_pairs_noalloc(lsb_elem_t* d_a, lsb_elem_t* d_b, int64_t n, int digit_bits,
+                           void* stream);
+
 /* Profiling (the reference only times mySort as a whole with steady_clock,
  * mpi/mpi_lsbsort.cpp:731-745). When enabled, the library brackets each of
  * its own kernel launches with CUDA events recorded on the launching stream;

@@ -1,0 +1,58 @@
+"""lsb_sort_pairs_noalloc: the sort for callers that may not allocate device
+memory (a framework that owns all GPU memory through its own arena, a path
+that cannot take cudaMalloc's device-wide synchronisation). Its scratch is a
+fixed array inside the library, shared by every call and left holding the
+last call's contents, so this checks two calls in a row -- the second must
+not be disturbed by what the first left behind -- against lsb_sort_pairs,
+byte for byte. The file is named to be collected last."""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+import pytest
+
+from conftest import to_dev, to_np
+
+pytestmark = pytest.mark.gpu
+
+
+def _noalloc(lsb, torch, a: np.ndarray, bits: int) -> np.ndarray:
+    A = to_dev(a, torch)
+    B = torch.empty_like(A)
+    rc = lsb.load().lsb_sort_pairs_noalloc(ctypes.c_void_p(A.data_ptr()), ctypes.c_void_p(B.data_ptr()),
+                                           a.shape[0], bits,
+                                           ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+    assert rc == lsb.LSB_OK, lsb.status_string(rc)
+    return to_np(A)
+
+
+def _existing(lsb, torch, a: np.ndarray, bits: int) -> np.ndarray:
+    A = to_dev(a, torch)
+    B = torch.empty_like(A)
+    lsb.sort_pairs(A, B, bits)
+    return to_np(A)
+
+
+def test_noalloc_matches_sort_pairs_twice_in_a_row(lsb, cuda, oracle):
+    # large enough that the look-back ring wraps (tiles > ring slots), and a
+    # smaller second call that must not see the first call's ring entries
+    cases = [((1 << 22) + 3, oracle.DIST_UNIFORM, 8), (70001, oracle.DIST_ZIPF, 8),
+             ((1 << 22) + 3, oracle.DIST_NEARLY_SORTED, 5), (4097, oracle.DIST_LOW32, 8)]
+    for call in range(2):
+        for n, dist, bits in cases:
+            a = oracle.generate(n, dist, seed=100 + call)
+            got = _noalloc(lsb, cuda, a, bits)
+            assert np.array_equal(got, _existing(lsb, cuda, a, bits)), (call, n, dist, bits)
+
+
+def test_noalloc_rejects_beyond_its_limits(lsb, cuda):
+    L = lsb.load()
+    A = cuda.empty((1024, 2), dtype=cuda.int64, device="cuda")
+    B = cuda.empty_like(A)
+    s = ctypes.c_void_p(cuda.cuda.current_stream().cuda_stream)
+    pa, pb = ctypes.c_void_p(A.data_ptr()), ctypes.c_void_p(B.data_ptr())
+    assert L.lsb_sort_pairs_noalloc(pa, pb, 1024, 11, s) == lsb.LSB_ERR_TOO_LARGE
+    assert L.lsb_sort_pairs_noalloc(pa, pb, 1024, 16, s) == lsb.LSB_ERR_TOO_LARGE
+    assert L.lsb_sort_pairs_noalloc(pa, pb, 1 << 33, 8, s) == lsb.LSB_ERR_TOO_LARGE
+    assert L.lsb_sort_pairs_noalloc(pa, pa, 1024, 8, s) == lsb.LSB_ERR_OVERLAP
