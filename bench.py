@@ -290,6 +290,9 @@ def gpu_arm(args, ranks: Ranks):
     bad = lsb.verify(inp, A)
     if bad:
         raise RuntimeError(f"timed sort differs from the stable sort ({bad} violations)")
+    # look-back diagnostics of the last sort (control block words 10 and 11)
+    ctrl_words = ws[:64].cpu().numpy().view("<u4")
+    lookback = {"windows_read": int(ctrl_words[10]), "windows_polled": int(ctrl_words[11])}
 
     # per-kernel device times (separate, profiled steps; same work)
     lsb.profile_read()
@@ -336,31 +339,50 @@ def gpu_arm(args, ranks: Ranks):
                      "traffic": traffic, "traffic_source": traffic_src,
                      "algorithmic_bytes_per_launch": per_elem * n, "mean_launch_ms": round(dom_ms, 4),
                      "peak_source": peaks["source"]},
+        "kernel_passes": int(prof.get(dom, (0, 0))[0] / prof_steps) if dom.endswith("scatter") else None,
         "sort_roofline": {"algorithmic_bytes_per_element": algorithmic_bytes_per_element(bits, passes_run),
                           "achieved_gbs": round(sort_bytes / (ms_per_step / 1e3) / 1e9, 1),
                           "frac": round(sort_bytes / (ms_per_step / 1e3) / 1e9 / peaks["hbm_gbs"], 4)},
         "kernels": {k: {kk: round(vv, 4) for kk, vv in v.items()} for k, v in kernels.items()},
+        "lookback": lookback,
         "gpu_launches": int(round(launches_per_step * args.steps)),
         "clocks": clk,
     }
 
-    # side measurement: the 8-bit-digit configuration of the same input
-    if not args.no_extra and bits != 8:
-        ws8 = lsb.alloc_workspace(n, 8)
-        ev = []
-        for i in range(2 + 3):
-            A.copy_(inp)
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
-            lsb.sort_pairs(A, B, 8, workspace=ws8)
-            e1.record(stream)
-            if i >= 2:
-                ev.append((e0, e1))
-        torch.cuda.synchronize()
-        ms8 = statistics.mean(a.elapsed_time(b) for a, b in ev)
-        out["digit_bits_8"] = {"ms_per_step": round(ms8, 4), "value": round(n / (ms8 / 1e3) / 1e6, 3),
-                               "verify_violations": lsb.verify(inp, A)}
-        del ws8
+    # side measurements on the same input: 8-bit digits, and (for wide digits)
+    # the single-pass task kernel family instead of split sub-passes
+    def time_sorts(b: int, reps: int = 3, env: dict | None = None):
+        old = {k: os.environ.get(k) for k in (env or {})}
+        os.environ.update(env or {})
+        try:
+            wsx = lsb.alloc_workspace(n, b)
+            ev = []
+            for i in range(2 + reps):
+                A.copy_(inp)
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                lsb.sort_pairs(A, B, b, workspace=wsx)
+                e1.record(stream)
+                if i >= 2:
+                    ev.append((e0, e1))
+            torch.cuda.synchronize()
+            ms = statistics.mean(a.elapsed_time(b_) for a, b_ in ev)
+            return {"ms_per_step": round(ms, 4), "value": round(n / (ms / 1e3) / 1e6, 3),
+                    "verify_violations": lsb.verify(inp, A)}
+        finally:
+            for k, v in old.items():
+                if v is None:
+                    os.environ.pop(k, None)
+                else:
+                    os.environ[k] = v
+
+    if not args.no_extra:
+        if bits != 8:
+            out["digit_bits_8"] = time_sorts(8)
+        if bits != 11:
+            out["digit_bits_11"] = time_sorts(11)
+        if bits in (12, 14, 16):
+            out["single_pass_task_family"] = time_sorts(bits, reps=2, env={"LSB_WIDE_DIGITS": "task"})
 
     # e2e through the host-buffer entry point
     if not args.no_e2e:

@@ -5,6 +5,7 @@
 // device verifier). The pass kernels live in lsb_onesweep.cu and lsb_task.cu.
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <vector>
@@ -88,10 +89,29 @@ static int pool_alloc(void** ptr, size_t bytes, cudaStream_t st) {
 // ---------------------------------------------------------------------------
 // workspace layout
 
-int plan_layout(int64_t n, int bits, int num_digits, Layout* L) {
+// How wide digits (12, 14, 16 bits) run inside lsb_sort_pairs: "split"
+// (default) executes each pass as two stable half-width onesweep sub-passes,
+// "task" as one pass of the task family. Read from LSB_WIDE_DIGITS.
+static bool wide_digits_split() {
+  const char* e = std::getenv("LSB_WIDE_DIGITS");
+  return !(e && std::strcmp(e, "task") == 0);
+}
+
+int plan_layout(int64_t n, int bits, int num_digits, Layout* L, bool allow_split) {
   DeviceInfo dev;
   if (int rc = current_device_info(&dev)) return rc;
   *L = Layout();
+  L->api_bits = bits;
+  L->sub = 1;
+  if (bits > 11 && allow_split && bits % 2 == 0 && bits <= 16 && wide_digits_split()) {
+    // a stable sort by digit d equals a stable sort by its low half, then by
+    // its high half: half-width digits 2d and 2d+1
+    const int half = bits / 2;
+    const int half_passes = (64 + half - 1) / half;
+    L->sub = 2;
+    num_digits = std::min(2 * num_digits, half_passes);
+    bits = half;
+  }
   L->bits = bits;
   L->num_digits = num_digits;
   L->n = (uint32_t)n;
@@ -129,6 +149,7 @@ int run_passes(Elem* X, Elem* Y, int first_digit, int target_parity, void* ws, c
                cudaStream_t st) {
   unsigned char* w = static_cast<unsigned char*>(ws);
   if (cudaMemsetAsync(w, 0, kCtrlBytes, st) != cudaSuccess) return LSB_ERR_CUDA;
+  first_digit *= L.sub;  // split wide digits: sub-digits 2d and 2d+1
   int rc = (L.family == Family::kOnesweep) ? onesweep_run(X, Y, first_digit, target_parity, w, L, st)
                                             : task_run(X, Y, first_digit, target_parity, w, L, st);
   if (rc) return rc == 1 ? LSB_ERR_INVALID_ARG : LSB_ERR_CUDA;
@@ -322,16 +343,20 @@ int lsb_num_passes(int digit_bits) {
 int lsb_workspace_bytes(int64_t n, int digit_bits, size_t* bytes) {
   if (!bytes || digit_bits < 1 || digit_bits > 16 || n < 0) return LSB_ERR_INVALID_ARG;
   if (n > LSB_MAX_ELEMENTS) return LSB_ERR_TOO_LARGE;
-  Layout L;
-  if (int rc = plan_layout(n, digit_bits, lsb_num_passes(digit_bits), &L)) return rc;
-  *bytes = L.total;
+  Layout Ls, Lp;
+  if (int rc = plan_layout(n, digit_bits, lsb_num_passes(digit_bits), &Ls, true)) return rc;
+  if (int rc = plan_layout(n, digit_bits, 1, &Lp, false)) return rc;
+  *bytes = std::max(Ls.total, Lp.total);
   return LSB_OK;
 }
 
 static int sort_or_pass(Elem* X, Elem* Y, int64_t n, int bits, int first_digit, int num_digits,
                         int target_parity, void* ws, size_t ws_bytes, cudaStream_t st) {
+  // a single pass must not write its source, so it never splits a wide digit
+  // (two sub-passes would end in the source buffer)
+  const bool allow_split = target_parity == 0;
   Layout L;
-  if (int rc = plan_layout(n, bits, num_digits, &L)) return rc;
+  if (int rc = plan_layout(n, bits, num_digits, &L, allow_split)) return rc;
   if (ws) {
     if (((uintptr_t)ws & 255u) != 0 || ws_bytes < L.total) return LSB_ERR_WORKSPACE;
     return run_passes(X, Y, first_digit, target_parity, ws, L, st);
@@ -428,10 +453,33 @@ int lsb_query(const void* d_workspace, void* stream, lsb_stats_t* stats) {
     return LSB_ERR_CUDA;
   std::memset(stats, 0, sizeof *stats);
   stats->device_status = (int32_t)c.error;
-  stats->passes_planned = (int32_t)c.num_passes;
-  stats->passes_run = (int32_t)c.passes_run;
-  stats->skipped_mask = c.skip_mask_lo;
   stats->final_copy = (int32_t)c.final_copy;
+  stats->digit_bits = (int32_t)c.api_bits;
+  stats->n = (int64_t)c.n;
+  // report in the caller's digits: a split wide digit is skipped only when
+  // both of its sub-passes were
+  const uint32_t sub = c.sub ? c.sub : 1u;
+  const int planned = c.api_bits ? lsb_num_passes((int)c.api_bits) : (int)c.num_passes;
+  auto kskip = [&](uint32_t p) -> bool {
+    if (p >= c.num_passes) return true;  // a sub-digit past bit 63
+    const uint32_t m = p < 32 ? c.skip_mask_lo : c.skip_mask_hi;
+    return (m >> (p & 31)) & 1u;
+  };
+  uint32_t mask = 0;
+  int run = 0;
+  const int digits = c.num_passes ? (int)((c.num_passes + sub - 1) / sub) : 0;
+  for (int d = 0; d < digits; d++) {
+    bool skipped = true;
+    for (uint32_t q = 0; q < sub; q++) skipped = skipped && kskip((uint32_t)d * sub + q);
+    if (skipped) {
+      if (d < 32) mask |= 1u << d;
+    } else {
+      run++;
+    }
+  }
+  stats->passes_planned = sub > 1 ? planned : (int32_t)c.num_passes;
+  stats->passes_run = run;
+  stats->skipped_mask = mask;
   return stats->device_status;
 }
 
@@ -441,7 +489,7 @@ int lsb_sort_pairs_host(lsb_elem_t* h_a, int64_t n, int digit_bits, void* stream
   if (n <= 1) return LSB_OK;
   cudaStream_t st = (cudaStream_t)stream;
   Layout L;
-  if (int rc = plan_layout(n, digit_bits, lsb_num_passes(digit_bits), &L)) return rc;
+  if (int rc = plan_layout(n, digit_bits, lsb_num_passes(digit_bits), &L, true)) return rc;
   const size_t bytes = (size_t)n * sizeof(Elem);
   void* buf = nullptr;
   if (int rc = pool_alloc(&buf, 2 * bytes + L.total + 256, st)) return rc;

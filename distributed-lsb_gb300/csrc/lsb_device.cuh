@@ -37,8 +37,12 @@ struct Ctrl {
   uint32_t skip_mask_hi;           // same for p in [32, 64)
   uint32_t passes_run;             // passes actually executed
   uint32_t final_copy;             // 1 if the result had to be copied back
-  uint32_t num_passes;             // planned passes
-  uint32_t pad0;
+  uint32_t num_passes;             // planned kernel passes
+  uint32_t api_bits;               // digit width the caller asked for
+  uint32_t sub;                    // kernel passes per caller digit (1, or 2 for a split wide digit)
+  uint32_t n;                      // elements
+  uint32_t lookback_steps;         // diagnostics: look-back windows read (all tiles, all passes)
+  uint32_t lookback_polls;         // diagnostics: windows that found a predecessor unpublished
   uint32_t parity[kMaxPasses + 1]; // parity[p]: 0 = pass p reads X, writes Y; 1 = reads Y, writes X
   uint32_t ticket[kMaxPasses];     // tile dispenser per pass (in-order tile dispatch)
 };
@@ -100,6 +104,31 @@ __device__ __forceinline__ uint32_t lanemask_lt() {
   uint32_t m;
   asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
   return m;
+}
+
+// Lanes of the warp whose `bits`-bit value v equals this lane's, from one
+// ballot per bit (ALU work instead of the match unit). `valid` lanes only
+// match valid lanes.
+__device__ __forceinline__ uint32_t warp_peers(uint32_t v, int bits, bool valid) {
+  const uint32_t vm = __ballot_sync(0xffffffffu, valid);
+  uint32_t peers = valid ? vm : ~vm;
+  for (int i = 0; i < bits; i++) {
+    const bool bit = (v >> i) & 1u;
+    const uint32_t b = __ballot_sync(0xffffffffu, bit);
+    peers &= bit ? b : ~b;
+  }
+  return peers;
+}
+template <int BITS>
+__device__ __forceinline__ uint32_t warp_peers_fixed(uint32_t v) {
+  uint32_t peers = 0xffffffffu;
+#pragma unroll
+  for (int i = 0; i < BITS; i++) {
+    const bool bit = (v >> i) & 1u;
+    const uint32_t b = __ballot_sync(0xffffffffu, bit);
+    peers &= bit ? b : ~b;
+  }
+  return peers;
 }
 
 // Look-back status word: [63:62] flag, [61:32] tag, [31:0] value.

@@ -33,7 +33,9 @@ enum class Family { kOnesweep = 0, kTask = 1 };
 // Byte offsets inside the caller's workspace (all 256-byte aligned).
 struct Layout {
   Family family = Family::kOnesweep;
-  int bits = 0;
+  int api_bits = 0;    // digit width the caller asked for
+  int sub = 1;         // kernel passes per caller digit (2 when a wide digit is split)
+  int bits = 0;        // digit width the kernels run with
   int num_digits = 0;  // passes covered by this call
   uint32_t n = 0;
   size_t total = 0;
@@ -52,7 +54,9 @@ struct Layout {
   uint32_t tasks = 0;
 };
 
-int plan_layout(int64_t n, int bits, int num_digits, Layout* out);
+// allow_split: digits of 12, 14 or 16 bits may run as two half-width
+// onesweep sub-passes each (sorts only; see lsb_capi.cu).
+int plan_layout(int64_t n, int bits, int num_digits, Layout* out, bool allow_split = false);
 
 // Runs passes [first_digit, first_digit + L.num_digits) over buffers X and Y.
 // Pass data starts in X. When target_parity is 0 the result ends in X (sort),

@@ -23,10 +23,16 @@ namespace lsb {
 constexpr int kHistThreads = 512;
 constexpr int kHistUnroll = 4;
 
+// BITS > 0: digit width and digit count fixed at compile time (digits
+// 0..P-1 of a whole sort); BITS == 0: runtime width and digit range.
+template <int BITS>
 __global__ void __launch_bounds__(kHistThreads)
-    k_hist_digits(const Elem* __restrict__ data, uint32_t n, int bits, int first_digit,
-                  int num_digits, uint32_t* __restrict__ ghist) {
+    k_hist_digits(const Elem* __restrict__ data, uint32_t n, int bits_rt, int first_digit_rt,
+                  int num_digits_rt, uint32_t* __restrict__ ghist) {
   extern __shared__ uint32_t h[];
+  const int bits = BITS > 0 ? BITS : bits_rt;
+  const int first_digit = BITS > 0 ? 0 : first_digit_rt;
+  const int num_digits = BITS > 0 ? (64 + BITS - 1) / BITS : num_digits_rt;
   const uint32_t nbins = 1u << bits, mask = nbins - 1u;
   const uint32_t total_bins = (uint32_t)num_digits * nbins;
   for (uint32_t i = threadIdx.x; i < total_bins; i += blockDim.x) h[i] = 0u;
@@ -34,32 +40,50 @@ __global__ void __launch_bounds__(kHistThreads)
   const uint32_t lane = lane_id();
   const uint64_t warps_total = (uint64_t)gridDim.x * (blockDim.x >> 5);
   const uint64_t gw = (uint64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  const uint64_t step = warps_total * 32u * kHistUnroll;
-  for (uint64_t base = gw * 32u * kHistUnroll; base < n; base += step) {
-    Elem e[kHistUnroll];
-    bool valid[kHistUnroll];
+  const uint64_t chunk = 32u * kHistUnroll;
+  const uint64_t full_end = (uint64_t)n / chunk * chunk;  // whole warp chunks
+  for (uint64_t base = gw * chunk; base < full_end; base += warps_total * chunk) {
+    uint64_t key[kHistUnroll];
+#pragma unroll
+    for (int u = 0; u < kHistUnroll; u++) key[u] = load_elem_stream(data + base + (uint64_t)u * 32u + lane).key;
 #pragma unroll
     for (int u = 0; u < kHistUnroll; u++) {
-      const uint64_t i = base + (uint64_t)u * 32u + lane;
-      valid[u] = i < n;
-      if (valid[u]) e[u] = load_elem_stream(data + i);
-    }
+      // bits in which some lane's key differs from lane 0's: a digit whose
+      // bits are all clear there is the same in the whole warp, and one
+      // shared atomic of 32 replaces 32 conflicting ones (skewed inputs)
+      const uint64_t x = key[u] ^ __shfl_sync(0xffffffffu, key[u], 0);
+      const uint64_t diff = ((uint64_t)__reduce_or_sync(0xffffffffu, (uint32_t)(x >> 32)) << 32) |
+                            __reduce_or_sync(0xffffffffu, (uint32_t)x);
 #pragma unroll
-    for (int u = 0; u < kHistUnroll; u++) {
-      const uint32_t vmask = __ballot_sync(0xffffffffu, valid[u]);
-      if (vmask == 0u) break;  // warp-uniform
-      for (int dd = 0; dd < num_digits; dd++) {
-        const int shift = bits * (first_digit + dd);
-        const uint32_t d = valid[u] ? digit_of(e[u].key, shift, mask) : 0xffffffffu;
-        const uint32_t d0 = __shfl_sync(0xffffffffu, d, 0);
-        const uint32_t same = __ballot_sync(0xffffffffu, d == d0);
-        if (same == vmask) {  // whole warp on one digit: one shared atomic instead of 32
-          if (lane == 0) atomicAdd(&h[dd * nbins + d0], (uint32_t)__popc(vmask));
-        } else if (valid[u]) {
+      for (int dd = 0; dd < (BITS > 0 ? (64 + BITS - 1) / BITS : 1); dd++) {
+        if (BITS == 0) break;
+        const int shift = bits * dd;
+        const uint32_t d = digit_of(key[u], shift, mask);
+        if (digit_of(diff, shift, mask) == 0u) {
+          if (lane == 0) atomicAdd(&h[dd * nbins + d], 32u);
+        } else {
           atomicAdd(&h[dd * nbins + d], 1u);
         }
       }
+      if (BITS == 0) {
+        for (int dd = 0; dd < num_digits; dd++) {
+          const int shift = bits * (first_digit + dd);
+          const uint32_t d = digit_of(key[u], shift, mask);
+          if (digit_of(diff, shift, mask) == 0u) {
+            if (lane == 0) atomicAdd(&h[dd * nbins + d], 32u);
+          } else {
+            atomicAdd(&h[dd * nbins + d], 1u);
+          }
+        }
+      }
     }
+  }
+  // the partial chunk at the end, one element per thread
+  for (uint64_t i = full_end + (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t k = load_elem_stream(data + i).key;
+    for (int dd = 0; dd < num_digits; dd++)
+      atomicAdd(&h[dd * nbins + digit_of(k, bits * (first_digit + dd), mask)], 1u);
   }
   __syncthreads();
   for (uint32_t i = threadIdx.x; i < total_bins; i += blockDim.x) {
@@ -76,11 +100,14 @@ int histogram_u32(const Elem* data, uint32_t n, int bits, int first_digit, int n
   if (smem > (size_t)dev.max_smem_optin) return 1;
   if (cudaMemsetAsync(d_counts, 0, smem, st) != cudaSuccess) return 5;
   if (n == 0) return 0;
-  if (cudaFuncSetAttribute(k_hist_digits, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)smem) != cudaSuccess)
+  const bool whole = first_digit == 0 && num_digits == (64 + bits - 1) / bits;
+  auto kern = (whole && bits == 8) ? k_hist_digits<8> : (whole && bits == 11) ? k_hist_digits<11>
+                                                                              : k_hist_digits<0>;
+  if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+      cudaSuccess)
     return 5;
   int per_sm = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_hist_digits, kHistThreads, smem);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kHistThreads, smem);
   per_sm = std::max(per_sm, 1);
   // enough CTAs to keep every SM streaming, but no more than the work needs
   const uint64_t per_cta = (uint64_t)kHistThreads * kHistUnroll * 4u;
@@ -88,8 +115,7 @@ int histogram_u32(const Elem* data, uint32_t n, int bits, int first_digit, int n
   const uint32_t grid = (uint32_t)std::max<uint64_t>(
       1, std::min<uint64_t>(want, (uint64_t)dev.sm_count * per_sm));
   ProfScope prof("hist_digits", st);
-  k_hist_digits<<<grid, kHistThreads, smem, st>>>(data, n, bits, first_digit, num_digits,
-                                                  d_counts);
+  kern<<<grid, kHistThreads, smem, st>>>(data, n, bits, first_digit, num_digits, d_counts);
   return cudaPeekAtLastError() == cudaSuccess ? 0 : 5;
 }
 
@@ -100,7 +126,7 @@ constexpr int kPlanThreads = 1024;
 
 __global__ void __launch_bounds__(kPlanThreads)
     k_plan(const uint32_t* __restrict__ ghist, uint32_t* __restrict__ gstart, uint32_t n, int bits,
-           int num_digits, int target_parity, Ctrl* ctrl) {
+           int num_digits, int target_parity, int api_bits, int sub, Ctrl* ctrl) {
   __shared__ uint32_t wt[33];
   __shared__ uint32_t s_const[kMaxPasses];
   const uint32_t nbins = 1u << bits;
@@ -141,6 +167,9 @@ __global__ void __launch_bounds__(kPlanThreads)
     ctrl->passes_run = runs;
     ctrl->num_passes = (uint32_t)num_digits;
     ctrl->final_copy = (par != (uint32_t)target_parity) ? 1u : 0u;
+    ctrl->api_bits = (uint32_t)api_bits;
+    ctrl->sub = (uint32_t)sub;
+    ctrl->n = n;
   }
 }
 
@@ -153,13 +182,16 @@ __device__ __forceinline__ bool pass_skipped(const Ctrl* ctrl, int pass) {
 // the onesweep scatter
 
 // Waits until the 64-bit status word at p carries `tag` and a flag; returns
-// it, or returns 0 after kSpinLimit polls (and records the timeout).
+// it, or returns 0 after kSpinLimit polls (and records the timeout). Once any
+// wait of this launch has failed (ctrl->error set), every later wait returns
+// at once, so a failure costs one spin limit, not one per tile and digit.
 __device__ __forceinline__ uint64_t wait_status(const uint64_t* p, uint32_t tag, Ctrl* ctrl,
                                                 bool* timed_out) {
   uint32_t ns = 8;
   for (uint32_t it = 0; it < kSpinLimit; it++) {
     const uint64_t s = ld_relaxed_u64(p);
     if (status_tag(s) == tag && status_flag(s) != 0) return s;
+    if ((it & 63u) == 0u && error_raised(ctrl)) break;
     __nanosleep(ns);
     if (ns < 256) ns <<= 1;
   }
@@ -168,24 +200,85 @@ __device__ __forceinline__ uint64_t wait_status(const uint64_t* p, uint32_t tag,
   return 0;
 }
 
-template <int THREADS, int K>
-__global__ void __launch_bounds__(THREADS)
+// Sums the look-back of digit `b` for tile t: walks predecessors t-1, t-2, ...
+// four status words at a time (independent loads), adding aggregates until an
+// inclusive prefix is found. Returns the number of digit-b elements in tiles
+// [0, t). Bounded: a predecessor that stays unpublished for kSpinLimit polls
+// (or an error raised elsewhere) ends the walk with *timed_out set.
+constexpr int kLookbackWindow = 8;
+
+__device__ __forceinline__ uint32_t lookback_digit(const uint64_t* __restrict__ ring,
+                                                   uint32_t ring_tiles, uint32_t nbins, uint32_t b,
+                                                   int pass, uint32_t t, Ctrl* ctrl,
+                                                   bool* timed_out, uint32_t* steps,
+                                                   uint32_t* polls_out) {
+  uint32_t excl = 0;
+  int64_t j = (int64_t)t - 1;
+  uint32_t polls = 0, ns = 8;
+  while (j >= 0) {
+    constexpr int WN = kLookbackWindow;
+    const int cnt = j >= WN - 1 ? WN : (int)j + 1;
+    uint64_t s[WN];
+#pragma unroll
+    for (int q = 0; q < WN; q++)
+      if (q < cnt) s[q] = ld_relaxed_u64(ring + (size_t)((uint32_t)(j - q) % ring_tiles) * nbins + b);
+    *steps += 1;
+    int q = 0;
+    bool incl = false;
+#pragma unroll
+    for (int u = 0; u < WN; u++) {
+      if (u == q && q < cnt) {
+        const uint64_t e = s[u];
+        if (status_tag(e) == ring_tag(pass, (uint32_t)(j - u)) && status_flag(e) != 0) {
+          excl += (uint32_t)e;
+          q++;
+          if (status_flag(e) == kFlagIncl) incl = true;
+        }
+      }
+      if (incl) break;
+    }
+    if (incl) break;
+    j -= q;
+    if (q < cnt) {  // the nearest unconsumed predecessor has not published yet
+      if (++polls >= kSpinLimit || ((polls & 63u) == 0u && error_raised(ctrl))) {
+        record_error(ctrl, kStatusTimeout, kWhereLookback);
+        *timed_out = true;
+        break;
+      }
+      __nanosleep(ns);
+      if (ns < 256) ns <<= 1;
+    }
+  }
+  *polls_out += polls;
+  return excl;
+}
+
+// One pass over the tiles of the input (persistent CTAs, tiles in input order).
+// CNT: per-warp digit counter type (uint16_t when 2^b x warps x 4 bytes would
+// not fit beside the staging buffer; a tile never exceeds 65535 elements).
+// Each CTA takes its next tile from the ticket and issues that tile's loads as
+// soon as the current tile is staged in shared memory, so the loads are in
+// flight during the current tile's look-back and stores.
+template <int THREADS, int K, int MINB, typename CNT>
+__global__ void __launch_bounds__(THREADS, MINB)
     k_onesweep(Elem* __restrict__ X, Elem* __restrict__ Y, uint32_t n, int bits, int pass,
                int digit, const uint32_t* __restrict__ gstart, uint64_t* __restrict__ ring,
                uint32_t* __restrict__ done, uint32_t ring_tiles, Ctrl* ctrl) {
   constexpr int W = THREADS / 32;
+  constexpr int WP = W + 1;  // padded row: the lanes of a warp hit different banks
   constexpr uint32_t E = THREADS * K;
+  static_assert(E <= 65535, "16-bit counters");
   constexpr uint32_t kSentinel = 0xffffffffu;
   extern __shared__ __align__(16) unsigned char smem[];
-  __shared__ uint32_t s_tile, s_err;
+  __shared__ uint32_t s_tile, s_next, s_err;
   __shared__ uint32_t s_wt[33];
 
   if (pass_skipped(ctrl, pass)) return;
   const uint32_t nbins = 1u << bits, mask = nbins - 1u;
   const int shift = bits * digit;  // `pass` indexes this call's passes, `digit` the key
-  const size_t stage_bytes = std::max<size_t>((size_t)E * sizeof(Elem), (size_t)nbins * W * 4u);
-  Elem* stage = reinterpret_cast<Elem*>(smem);        // tile in digit order
-  uint32_t* wcnt = reinterpret_cast<uint32_t*>(smem); // per-warp counters [bin][warp], aliased
+  const size_t stage_bytes = std::max<size_t>((size_t)E * sizeof(Elem), (size_t)nbins * WP * sizeof(CNT));
+  Elem* stage = reinterpret_cast<Elem*>(smem);   // tile in digit order
+  CNT* wcnt = reinterpret_cast<CNT*>(smem);      // per-warp counters [bin][WP], aliased
   uint32_t* base = reinterpret_cast<uint32_t*>(smem + stage_bytes);  // [nbins]
   uint32_t* tcount = base + nbins;                                    // [nbins]
 
@@ -196,78 +289,54 @@ __global__ void __launch_bounds__(THREADS)
   const uint32_t warp = threadIdx.x >> 5, lane = lane_id();
   const uint32_t lt = lanemask_lt();
 
-  for (;;) {
-    if (threadIdx.x == 0) {
-      s_tile = atomicAdd(&ctrl->ticket[pass], 1u);
-      s_err = 0u;
-    }
-    __syncthreads();
-    const uint32_t t = s_tile;
-    if (t >= num_tiles) break;
+  Elem v[K];
+  uint32_t d[K];
+  // loads tile `t` warp-striped: item k of lane l in warp w is tile element
+  // w*32*K + k*32 + l (coalesced 512-byte warp loads)
+  auto load_tile = [&](uint32_t t) {
     const uint32_t tile_begin = t * E;
-    const uint32_t tile_len = min(E, n - tile_begin);
-
-    // 1. load the tile, warp-striped: item k of lane l in warp w is tile
-    //    element w*32*K + k*32 + l (coalesced 512-byte warp loads)
-    Elem v[K];
-    uint32_t d[K];
+    const uint32_t len = min(E, n - tile_begin);
 #pragma unroll
     for (int k = 0; k < K; k++) {
       const uint32_t s = warp * 32u * K + (uint32_t)k * 32u + lane;
-      if (s < tile_len) {
+      if (s < len) {
         v[k] = load_elem_stream(src + tile_begin + s);
         d[k] = digit_of(v[k].key, shift, mask);
       } else {
         d[k] = kSentinel;
       }
     }
-    for (uint32_t i = threadIdx.x; i < nbins * W; i += THREADS) wcnt[i] = 0u;
+  };
+
+  if (threadIdx.x == 0) s_tile = atomicAdd(&ctrl->ticket[pass], 1u);
+  __syncthreads();
+  uint32_t t = s_tile;
+  if (t < num_tiles) load_tile(t);
+  uint32_t lb_steps = 0, lb_polls = 0;
+
+  while (t < num_tiles) {
+    const uint32_t tile_len = min(E, n - t * E);
+    if (threadIdx.x == 0) s_err = 0u;
+    for (uint32_t i = threadIdx.x; i < nbins * WP; i += THREADS) wcnt[i] = 0;
     __syncthreads();
 
-    // 2. stable rank inside each warp: peers with the same digit, in item order
+    // 1. stable rank inside each warp: peers with the same digit, in item order
     uint32_t r[K];
 #pragma unroll
     for (int k = 0; k < K; k++) {
-      const uint32_t peers = __match_any_sync(0xffffffffu, d[k]);
+      const uint32_t peers = warp_peers(d[k], bits, d[k] != kSentinel);
       uint32_t c = 0;
-      if (d[k] != kSentinel) c = wcnt[d[k] * W + warp];
+      if (d[k] != kSentinel) c = wcnt[d[k] * WP + warp];
       r[k] = c + __popc(peers & lt);
       __syncwarp();
       if (d[k] != kSentinel && lane == (uint32_t)(__ffs(peers) - 1))
-        wcnt[d[k] * W + warp] = c + __popc(peers);
+        wcnt[d[k] * WP + warp] = (CNT)(c + __popc(peers));
       __syncwarp();
     }
     __syncthreads();
 
-    // 3. exclusive scan of the counters in [digit][warp] order: the start of
-    //    each (digit, warp) group in the digit-sorted tile
-    {
-      const uint32_t entries = nbins * W;
-      const uint32_t per = (entries + THREADS - 1) / THREADS;
-      const uint32_t lo = min(threadIdx.x * per, entries), hi = min(lo + per, entries);
-      uint32_t sum = 0;
-      for (uint32_t i = lo; i < hi; i++) sum += wcnt[i];
-      uint32_t tot;
-      uint32_t ex = block_exclusive_scan(sum, s_wt, &tot);
-      for (uint32_t i = lo; i < hi; i++) {
-        const uint32_t c = wcnt[i];
-        wcnt[i] = ex;
-        ex += c;
-      }
-    }
-    __syncthreads();
-    for (uint32_t b = threadIdx.x; b < nbins; b += THREADS) {
-      const uint32_t st = wcnt[b * W];
-      const uint32_t en = (b + 1 < nbins) ? wcnt[(b + 1) * W] : tile_len;
-      tcount[b] = en - st;
-      base[b] = st;
-    }
-#pragma unroll
-    for (int k = 0; k < K; k++)
-      if (d[k] != kSentinel) r[k] += wcnt[d[k] * W + warp];
-    __syncthreads();
-
-    // 4. decoupled look-back per digit
+    // 2. the tile's count of every digit, published at once so that later
+    //    tiles can use it while this one is still working
     const uint32_t slot = t % ring_tiles;
     const uint32_t tag = ring_tag(pass, t);
     bool timed_out = false;
@@ -282,7 +351,7 @@ __global__ void __launch_bounds__(THREADS)
         const uint32_t want = ring_tag(pass, y);
         uint32_t ns = 8, it = 0;
         while (ld_acquire_u32(done + (y % ring_tiles)) < want) {
-          if (++it >= kSpinLimit) {
+          if (++it >= kSpinLimit || ((it & 63u) == 0u && error_raised(ctrl))) {
             record_error(ctrl, kStatusTimeout, kWhereRingReuse);
             timed_out = true;
             break;
@@ -292,22 +361,57 @@ __global__ void __launch_bounds__(THREADS)
         }
         if (timed_out) break;
       }
-      __syncthreads();
+      __syncthreads();  // every reader of the old tile is done before any thread overwrites it
     }
     uint64_t* my = ring + (size_t)slot * nbins;
-    for (uint32_t b = threadIdx.x; b < nbins; b += THREADS)
-      st_relaxed_u64(my + b, pack_status(t == 0 ? kFlagIncl : kFlagAgg, tag, tcount[b]));
+    for (uint32_t b = threadIdx.x; b < nbins; b += THREADS) {
+      uint32_t c = 0;
+#pragma unroll
+      for (int w = 0; w < W; w++) c += wcnt[b * WP + w];
+      tcount[b] = c;
+      st_relaxed_u64(my + b, pack_status(t == 0 ? kFlagIncl : kFlagAgg, tag, c));
+    }
+
+    // 3. exclusive scan of the counters in [digit][warp] order: the start of
+    //    each (digit, warp) group in the digit-sorted tile
+    {
+      const uint32_t entries = nbins * W;
+      const uint32_t per = (entries + THREADS - 1) / THREADS;
+      const uint32_t lo = min(threadIdx.x * per, entries), hi = min(lo + per, entries);
+      uint32_t sum = 0;
+      // logical entry i = (bin i / W, warp i % W) lives at (i / W) * WP + i % W
+      for (uint32_t i = lo; i < hi; i++) sum += wcnt[(i / W) * WP + i % W];
+      uint32_t tot;
+      uint32_t ex = block_exclusive_scan(sum, s_wt, &tot);
+      for (uint32_t i = lo; i < hi; i++) {
+        CNT* p = &wcnt[(i / W) * WP + i % W];
+        const uint32_t c = *p;
+        *p = (CNT)ex;
+        ex += c;
+      }
+    }
+    __syncthreads();
+    for (uint32_t b = threadIdx.x; b < nbins; b += THREADS) base[b] = wcnt[b * WP];
+#pragma unroll
+    for (int k = 0; k < K; k++)
+      if (d[k] != kSentinel) r[k] += wcnt[d[k] * WP + warp];
+    if (threadIdx.x == 0) s_next = atomicAdd(&ctrl->ticket[pass], 1u);
+    __syncthreads();
+
+    // 4. stage the tile in digit order (the counters are dead: stage aliases
+    //    them), then start loading the next tile into the freed registers
+#pragma unroll
+    for (int k = 0; k < K; k++)
+      if (d[k] != kSentinel) stage[r[k]] = v[k];
+    const uint32_t t_next = s_next;
+    if (t_next < num_tiles) load_tile(t_next);
+
+    // 5. decoupled look-back per digit
     for (uint32_t b = threadIdx.x; b < nbins; b += THREADS) {
       uint32_t excl = 0;
       if (t > 0) {
-        uint32_t j = t - 1;
-        for (;;) {
-          const uint64_t s = wait_status(ring + (size_t)(j % ring_tiles) * nbins + b,
-                                         ring_tag(pass, j), ctrl, &timed_out);
-          excl += (uint32_t)s;
-          if (status_flag(s) == kFlagIncl || timed_out || j == 0) break;
-          j--;
-        }
+        excl = lookback_digit(ring, ring_tiles, nbins, b, pass, t, ctrl, &timed_out, &lb_steps,
+                              &lb_polls);
         st_relaxed_u64(my + b, pack_status(kFlagIncl, tag, excl + tcount[b]));
       }
       base[b] = gstart[b] + excl - base[b];  // dst = base[digit] + sorted position
@@ -319,11 +423,7 @@ __global__ void __launch_bounds__(THREADS)
       st_release_u32(done + slot, tag);  // look-back of tile t finished
     }
 
-    // 5. stage the tile in digit order, then write runs of equal digits
-#pragma unroll
-    for (int k = 0; k < K; k++)
-      if (d[k] != kSentinel) stage[r[k]] = v[k];
-    __syncthreads();
+    // 6. write runs of equal digits with coalesced 16-byte stores
     if (!s_err) {
       for (uint32_t pos = threadIdx.x; pos < tile_len; pos += THREADS) {
         const Elem e = stage[pos];
@@ -332,40 +432,54 @@ __global__ void __launch_bounds__(THREADS)
       }
     }
     __syncthreads();
+    t = t_next;
   }
+  if (lb_steps) atomicAdd(&ctrl->lookback_steps, lb_steps);
+  if (lb_polls) atomicAdd(&ctrl->lookback_polls, lb_polls);
 }
 
-// Two configurations: up to 256 digits (512 threads x 8 items) and up to 2048
-// digits (256 threads x 16 items); both tiles hold 4096 elements.
-constexpr int kSmallThreads = 512, kSmallK = 8;
-constexpr int kLargeThreads = 256, kLargeK = 16;
+// Configuration: one 512-thread CTA per SM, 16 items per thread (8192-element
+// tiles). Large tiles keep the tile dispatch rate low, which keeps the
+// look-back shallow (its depth is about dispatch rate x look-back latency).
+// Counters are 32-bit up to 256 digits and 16-bit up to 2048 digits.
+struct OnesweepCfg {
+  int threads, k;
+  size_t cnt_bytes;
+};
+static OnesweepCfg onesweep_cfg(int bits) {
+  return bits <= 8 ? OnesweepCfg{512, 16, 4} : OnesweepCfg{512, 16, 2};
+}
+#define LSB_ONESWEEP_SMALL k_onesweep<512, 16, 1, uint32_t>
+#define LSB_ONESWEEP_LARGE k_onesweep<512, 16, 1, uint16_t>
 
 uint32_t onesweep_tile_elems(int bits) {
-  return bits <= 8 ? (uint32_t)(kSmallThreads * kSmallK) : (uint32_t)(kLargeThreads * kLargeK);
+  const OnesweepCfg c = onesweep_cfg(bits);
+  return (uint32_t)(c.threads * c.k);
 }
 
 static size_t onesweep_smem(int bits) {
+  const OnesweepCfg c = onesweep_cfg(bits);
   const size_t nbins = (size_t)1 << bits;
-  const int threads = bits <= 8 ? kSmallThreads : kLargeThreads;
-  const size_t E = onesweep_tile_elems(bits);
-  return std::max(E * sizeof(Elem), nbins * (threads / 32) * 4u) + 2u * nbins * 4u;
+  const size_t E = (size_t)c.threads * c.k;
+  return std::max(E * sizeof(Elem), nbins * (c.threads / 32 + 1) * c.cnt_bytes) + 2u * nbins * 4u;
 }
 
-template <int THREADS, int K>
-static uint32_t grid_for(size_t smem, const DeviceInfo& dev, uint32_t n) {
-  auto kern = k_onesweep<THREADS, K>;
+template <typename Kern>
+static uint32_t grid_for(Kern kern, int threads, uint32_t tile, size_t smem, const DeviceInfo& dev,
+                         uint32_t n) {
   cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   int per_sm = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, THREADS, smem);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem);
   per_sm = std::max(per_sm, 1);
-  const uint32_t tiles = (n + THREADS * K - 1) / (THREADS * K);
+  const uint32_t tiles = (n + tile - 1) / tile;
   return std::max<uint32_t>(1, std::min<uint32_t>(tiles, (uint32_t)(dev.sm_count * per_sm)));
 }
 
 uint32_t onesweep_grid(int bits, const DeviceInfo& dev, uint32_t n) {
   const size_t smem = onesweep_smem(bits);
-  return bits <= 8 ? grid_for<kSmallThreads, kSmallK>(smem, dev, n)
-                   : grid_for<kLargeThreads, kLargeK>(smem, dev, n);
+  const uint32_t tile = onesweep_tile_elems(bits);
+  return bits <= 8 ? grid_for(LSB_ONESWEEP_SMALL, 512, tile, smem, dev, n)
+                   : grid_for(LSB_ONESWEEP_LARGE, 512, tile, smem, dev, n);
 }
 
 // ---------------------------------------------------------------------------
@@ -413,7 +527,7 @@ int onesweep_run(Elem* X, Elem* Y, int first_digit, int target_parity, unsigned 
   {
     ProfScope prof("plan", st);
     k_plan<<<1, kPlanThreads, 0, st>>>(hist, gstart, L.n, L.bits, L.num_digits, target_parity,
-                                       ctrl);
+                                       L.api_bits, L.sub, ctrl);
   }
   if (cudaPeekAtLastError() != cudaSuccess) return 5;
   const size_t smem = onesweep_smem(L.bits);
@@ -423,11 +537,11 @@ int onesweep_run(Elem* X, Elem* Y, int first_digit, int target_parity, unsigned 
     const uint32_t* gs = gstart + (size_t)p * nbins;
     ProfScope prof("onesweep_scatter", st);
     if (L.bits <= 8) {
-      k_onesweep<kSmallThreads, kSmallK><<<L.grid, kSmallThreads, smem, st>>>(
-          X, Y, L.n, L.bits, p, first_digit + p, gs, ring, done, L.ring_tiles, ctrl);
+      LSB_ONESWEEP_SMALL<<<L.grid, 512, smem, st>>>(X, Y, L.n, L.bits, p, first_digit + p, gs,
+                                                    ring, done, L.ring_tiles, ctrl);
     } else {
-      k_onesweep<kLargeThreads, kLargeK><<<L.grid, kLargeThreads, smem, st>>>(
-          X, Y, L.n, L.bits, p, first_digit + p, gs, ring, done, L.ring_tiles, ctrl);
+      LSB_ONESWEEP_LARGE<<<L.grid, 512, smem, st>>>(X, Y, L.n, L.bits, p, first_digit + p, gs,
+                                                    ring, done, L.ring_tiles, ctrl);
     }
     if (cudaPeekAtLastError() != cudaSuccess) return 5;
   }

@@ -56,18 +56,28 @@ __global__ void __launch_bounds__(kCountThreads)
     const uint32_t sub_end = std::min<uint32_t>(end, sub + kCountSub);
     for (uint32_t i = threadIdx.x; i < words; i += blockDim.x) packed[i] = 0u;
     __syncthreads();
-    for (uint32_t b0 = sub + warp * 32u; b0 < sub_end; b0 += nwarps * 32u) {
-      const uint32_t i = b0 + lane;
-      const bool valid = i < sub_end;
-      const uint32_t vmask = __ballot_sync(0xffffffffu, valid);
-      uint32_t d = 0xffffffffu;
-      if (valid) d = digit_of(load_elem_stream(src + i).key, shift, mask);
-      const uint32_t d0 = __shfl_sync(0xffffffffu, d, 0);
-      const uint32_t same = __ballot_sync(0xffffffffu, d == d0);
-      if (same == vmask) {
-        if (lane == 0) atomicAdd(&packed[d0 >> 1], (uint32_t)__popc(vmask) << ((d0 & 1u) * 16u));
-      } else if (valid) {
-        atomicAdd(&packed[d >> 1], 1u << ((d & 1u) * 16u));
+    constexpr int U = 4;  // independent 16-byte loads per lane in flight
+    for (uint32_t b0 = sub + warp * 32u * U; b0 < sub_end; b0 += nwarps * 32u * U) {
+      uint64_t key[U];
+      bool valid[U];
+#pragma unroll
+      for (int u = 0; u < U; u++) {
+        const uint32_t i = b0 + (uint32_t)u * 32u + lane;
+        valid[u] = i < sub_end;
+        if (valid[u]) key[u] = load_elem_stream(src + i).key;
+      }
+#pragma unroll
+      for (int u = 0; u < U; u++) {
+        const uint32_t vmask = __ballot_sync(0xffffffffu, valid[u]);
+        if (vmask == 0u) break;  // warp-uniform
+        const uint32_t d = valid[u] ? digit_of(key[u], shift, mask) : 0xffffffffu;
+        const uint32_t d0 = __shfl_sync(0xffffffffu, d, 0);
+        const uint32_t same = __ballot_sync(0xffffffffu, d == d0);
+        if (same == vmask) {
+          if (lane == 0) atomicAdd(&packed[d0 >> 1], (uint32_t)__popc(vmask) << ((d0 & 1u) * 16u));
+        } else if (valid[u]) {
+          atomicAdd(&packed[d >> 1], 1u << ((d & 1u) * 16u));
+        }
       }
     }
     __syncthreads();
@@ -145,6 +155,9 @@ __global__ void __launch_bounds__(kPlanThreads16)
     }
     if (pass == num_digits - 1) {
       ctrl->num_passes = (uint32_t)num_digits;
+      ctrl->api_bits = (uint32_t)__popc(nbins - 1u);
+      ctrl->sub = 1u;
+      ctrl->n = n;
       ctrl->final_copy = (ctrl->parity[pass + 1] != (uint32_t)target_parity) ? 1u : 0u;
     }
   }
@@ -174,16 +187,17 @@ template <int THREADS, int K>
 __device__ __forceinline__ void block_rank8(const uint32_t (&key8)[K], uint32_t (&r)[K],
                                             uint32_t* cnt, uint32_t* wt) {
   constexpr int W = THREADS / 32;
+  constexpr int WP = W + 1;  // padded row: the lanes of a warp hit different banks
   const uint32_t warp = threadIdx.x >> 5, lane = lane_id(), lt = lanemask_lt();
-  for (uint32_t i = threadIdx.x; i < 256u * W; i += THREADS) cnt[i] = 0u;
+  for (uint32_t i = threadIdx.x; i < 256u * WP; i += THREADS) cnt[i] = 0u;
   __syncthreads();
 #pragma unroll
   for (int k = 0; k < K; k++) {
-    const uint32_t peers = __match_any_sync(0xffffffffu, key8[k]);
-    const uint32_t c = cnt[key8[k] * W + warp];
+    const uint32_t peers = warp_peers_fixed<8>(key8[k]);
+    const uint32_t c = cnt[key8[k] * WP + warp];
     r[k] = c + __popc(peers & lt);
     __syncwarp();
-    if (lane == (uint32_t)(__ffs(peers) - 1)) cnt[key8[k] * W + warp] = c + __popc(peers);
+    if (lane == (uint32_t)(__ffs(peers) - 1)) cnt[key8[k] * WP + warp] = c + __popc(peers);
     __syncwarp();
   }
   __syncthreads();
@@ -193,18 +207,20 @@ __device__ __forceinline__ void block_rank8(const uint32_t (&key8)[K], uint32_t 
     const uint32_t lo = std::min<uint32_t>(threadIdx.x * per, entries);
     const uint32_t hi = std::min<uint32_t>(lo + per, entries);
     uint32_t sum = 0;
-    for (uint32_t i = lo; i < hi; i++) sum += cnt[i];
+    // logical entry i = (digit i / W, warp i % W) lives at (i / W) * WP + i % W
+    for (uint32_t i = lo; i < hi; i++) sum += cnt[(i / W) * WP + i % W];
     uint32_t tot;
     uint32_t ex = block_exclusive_scan(sum, wt, &tot);
     for (uint32_t i = lo; i < hi; i++) {
-      const uint32_t c = cnt[i];
-      cnt[i] = ex;
+      uint32_t* p = &cnt[(i / W) * WP + i % W];
+      const uint32_t c = *p;
+      *p = ex;
       ex += c;
     }
   }
   __syncthreads();
 #pragma unroll
-  for (int k = 0; k < K; k++) r[k] += cnt[key8[k] * W + warp];
+  for (int k = 0; k < K; k++) r[k] += cnt[key8[k] * WP + warp];
   __syncthreads();
 }
 
@@ -247,9 +263,10 @@ __global__ void __launch_bounds__(kScatThreads)
                    int digit, uint32_t* __restrict__ table, uint32_t task_len, Ctrl* ctrl) {
   constexpr int THREADS = kScatThreads, K = kScatK, W = THREADS / 32;
   constexpr uint32_t E = kScatTile;
-  __shared__ uint32_t cnt[256 * W];  // rank counters, later run bases (E entries)
-  __shared__ uint32_t packA[E];      // round-1 output, later dst per input position
-  __shared__ uint32_t packB[E];      // digit-sorted (digit << 16 | input position)
+  extern __shared__ __align__(16) uint32_t scat_smem[];
+  uint32_t* cnt = scat_smem;              // [256 * (W+1)] rank counters, later run bases (E entries)
+  uint32_t* packA = cnt + 256 * (W + 1);  // [E] round-1 output, later dst per input position
+  uint32_t* packB = packA + E;            // [E] digit-sorted (digit << 16 | input position)
   __shared__ uint32_t wt[33];
   static_assert(256 * W >= (int)E, "run bases alias the rank counters");
   uint32_t* runbase = cnt;
@@ -355,10 +372,17 @@ __global__ void __launch_bounds__(kScatThreads)
 // ---------------------------------------------------------------------------
 // driver
 
+constexpr size_t kScatSmem = (256u * (kScatThreads / 32 + 1) + 2u * kScatTile) * 4u;
+
+static void scatter_smem_attr() {
+  cudaFuncSetAttribute(k_task_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kScatSmem);
+}
+
 uint32_t task_count(const DeviceInfo& dev, uint32_t n) {
   // one task per resident scatter CTA, but at least 64 Ki elements per task
   int per_sm = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_task_scatter, kScatThreads, 0);
+  scatter_smem_attr();
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_task_scatter, kScatThreads, kScatSmem);
   per_sm = std::max(per_sm, 1);
   const uint32_t by_size = std::max<uint32_t>(1u, (uint32_t)(((uint64_t)n + 65535u) / 65536u));
   return std::max<uint32_t>(1u, std::min<uint32_t>(by_size, (uint32_t)(dev.sm_count * per_sm)));
@@ -399,6 +423,7 @@ int task_run(Elem* X, Elem* Y, int first_digit, int target_parity, unsigned char
   const uint32_t nbins = 1u << L.bits;
   const uint32_t task_len = (uint32_t)(((uint64_t)L.n + L.tasks - 1) / L.tasks);
   const uint32_t dgrid = (nbins + 255) / 256;
+  scatter_smem_attr();
   for (int p = 0; p < L.num_digits; p++) {
     const int digit = first_digit + p;
     if (int rc = launch_count(X, Y, L.n, L.bits, p, digit, table, L.tasks, task_len, ctrl, st))
@@ -418,7 +443,7 @@ int task_run(Elem* X, Elem* Y, int first_digit, int target_parity, unsigned char
     }
     {
       ProfScope prof("task_scatter", st);
-      k_task_scatter<<<L.tasks, kScatThreads, 0, st>>>(X, Y, L.n, L.bits, p, digit, table,
+      k_task_scatter<<<L.tasks, kScatThreads, kScatSmem, st>>>(X, Y, L.n, L.bits, p, digit, table,
                                                        task_len, ctrl);
     }
     if (cudaPeekAtLastError() != cudaSuccess) return 5;
