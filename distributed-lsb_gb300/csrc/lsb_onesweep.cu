@@ -12,6 +12,7 @@
 // the tile in digit order in shared memory and writes runs of equal digits
 // with coalesced 16-byte stores.
 #include <algorithm>
+#include <cstdlib>
 
 #include "lsb_internal.h"
 
@@ -259,9 +260,11 @@ __device__ __forceinline__ uint32_t lookback_digit(const uint64_t* __restrict__ 
 // Each CTA takes its next tile from the ticket and issues that tile's loads as
 // soon as the current tile is staged in shared memory, so the loads are in
 // flight during the current tile's look-back and stores.
-template <int THREADS, int K, int MINB, typename CNT>
+// BITS > 0 fixes the digit width at compile time (8 and 11: the common widths);
+// BITS == 0 takes it from `bits_rt`.
+template <int THREADS, int K, int MINB, typename CNT, int BITS>
 __global__ void __launch_bounds__(THREADS, MINB)
-    k_onesweep(Elem* __restrict__ X, Elem* __restrict__ Y, uint32_t n, int bits, int pass,
+    k_onesweep(Elem* __restrict__ X, Elem* __restrict__ Y, uint32_t n, int bits_rt, int pass,
                int digit, const uint32_t* __restrict__ gstart, uint64_t* __restrict__ ring,
                uint32_t* __restrict__ done, uint32_t ring_tiles, Ctrl* ctrl) {
   constexpr int W = THREADS / 32;
@@ -274,6 +277,7 @@ __global__ void __launch_bounds__(THREADS, MINB)
   __shared__ uint32_t s_wt[33];
 
   if (pass_skipped(ctrl, pass)) return;
+  const int bits = BITS > 0 ? BITS : bits_rt;
   const uint32_t nbins = 1u << bits, mask = nbins - 1u;
   const int shift = bits * digit;  // `pass` indexes this call's passes, `digit` the key
   const size_t stage_bytes = std::max<size_t>((size_t)E * sizeof(Elem), (size_t)nbins * WP * sizeof(CNT));
@@ -296,14 +300,22 @@ __global__ void __launch_bounds__(THREADS, MINB)
   auto load_tile = [&](uint32_t t) {
     const uint32_t tile_begin = t * E;
     const uint32_t len = min(E, n - tile_begin);
+    const Elem* p = src + tile_begin + warp * 32u * K + lane;
+    if (len == E) {
 #pragma unroll
-    for (int k = 0; k < K; k++) {
-      const uint32_t s = warp * 32u * K + (uint32_t)k * 32u + lane;
-      if (s < len) {
-        v[k] = load_elem_stream(src + tile_begin + s);
-        d[k] = digit_of(v[k].key, shift, mask);
-      } else {
-        d[k] = kSentinel;
+      for (int k = 0; k < K; k++) v[k] = load_elem_stream(p + k * 32);
+#pragma unroll
+      for (int k = 0; k < K; k++) d[k] = digit_of(v[k].key, shift, mask);
+    } else {
+#pragma unroll
+      for (int k = 0; k < K; k++) {
+        const uint32_t s = warp * 32u * K + (uint32_t)k * 32u + lane;
+        if (s < len) {
+          v[k] = load_elem_stream(p + k * 32);
+          d[k] = digit_of(v[k].key, shift, mask);
+        } else {
+          d[k] = kSentinel;
+        }
       }
     }
   };
@@ -321,17 +333,32 @@ __global__ void __launch_bounds__(THREADS, MINB)
     __syncthreads();
 
     // 1. stable rank inside each warp: peers with the same digit, in item order
+    const bool full = tile_len == E;  // every item valid: no sentinel tests
     uint32_t r[K];
+    if (full) {
 #pragma unroll
-    for (int k = 0; k < K; k++) {
-      const uint32_t peers = warp_peers(d[k], bits, d[k] != kSentinel);
-      uint32_t c = 0;
-      if (d[k] != kSentinel) c = wcnt[d[k] * WP + warp];
-      r[k] = c + __popc(peers & lt);
-      __syncwarp();
-      if (d[k] != kSentinel && lane == (uint32_t)(__ffs(peers) - 1))
-        wcnt[d[k] * WP + warp] = (CNT)(c + __popc(peers));
-      __syncwarp();
+      for (int k = 0; k < K; k++) {
+        const uint32_t peers = BITS > 0 ? warp_peers_fixed<(BITS > 0 ? BITS : 1)>(d[k])
+                                        : warp_peers(d[k], bits, true);
+        CNT* cp = &wcnt[d[k] * WP + warp];
+        const uint32_t c = *cp;
+        r[k] = c + __popc(peers & lt);
+        __syncwarp();
+        if (lane == (uint32_t)(__ffs(peers) - 1)) *cp = (CNT)(c + __popc(peers));
+        __syncwarp();
+      }
+    } else {
+#pragma unroll
+      for (int k = 0; k < K; k++) {
+        const uint32_t peers = warp_peers(d[k], bits, d[k] != kSentinel);
+        uint32_t c = 0;
+        if (d[k] != kSentinel) c = wcnt[d[k] * WP + warp];
+        r[k] = c + __popc(peers & lt);
+        __syncwarp();
+        if (d[k] != kSentinel && lane == (uint32_t)(__ffs(peers) - 1))
+          wcnt[d[k] * WP + warp] = (CNT)(c + __popc(peers));
+        __syncwarp();
+      }
     }
     __syncthreads();
 
@@ -394,7 +421,7 @@ __global__ void __launch_bounds__(THREADS, MINB)
     for (uint32_t b = threadIdx.x; b < nbins; b += THREADS) base[b] = wcnt[b * WP];
 #pragma unroll
     for (int k = 0; k < K; k++)
-      if (d[k] != kSentinel) r[k] += wcnt[d[k] * WP + warp];
+      if (full || d[k] != kSentinel) r[k] += wcnt[d[k] * WP + warp];
     if (threadIdx.x == 0) s_next = atomicAdd(&ctrl->ticket[pass], 1u);
     __syncthreads();
 
@@ -402,7 +429,7 @@ __global__ void __launch_bounds__(THREADS, MINB)
     //    them), then start loading the next tile into the freed registers
 #pragma unroll
     for (int k = 0; k < K; k++)
-      if (d[k] != kSentinel) stage[r[k]] = v[k];
+      if (full || d[k] != kSentinel) stage[r[k]] = v[k];
     const uint32_t t_next = s_next;
     if (t_next < num_tiles) load_tile(t_next);
 
@@ -425,10 +452,20 @@ __global__ void __launch_bounds__(THREADS, MINB)
 
     // 6. write runs of equal digits with coalesced 16-byte stores
     if (!s_err) {
-      for (uint32_t pos = threadIdx.x; pos < tile_len; pos += THREADS) {
-        const Elem e = stage[pos];
-        const uint32_t o = base[digit_of(e.key, shift, mask)] + pos;
-        if (o < n) store_elem(dst + o, e);
+      if (full) {
+#pragma unroll 4
+        for (int k = 0; k < K; k++) {
+          const uint32_t pos = threadIdx.x + (uint32_t)k * THREADS;
+          const Elem e = stage[pos];
+          const uint32_t o = base[digit_of(e.key, shift, mask)] + pos;
+          if (o < n) store_elem(dst + o, e);
+        }
+      } else {
+        for (uint32_t pos = threadIdx.x; pos < tile_len; pos += THREADS) {
+          const Elem e = stage[pos];
+          const uint32_t o = base[digit_of(e.key, shift, mask)] + pos;
+          if (o < n) store_elem(dst + o, e);
+        }
       }
     }
     __syncthreads();
@@ -438,48 +475,295 @@ __global__ void __launch_bounds__(THREADS, MINB)
   if (lb_polls) atomicAdd(&ctrl->lookback_polls, lb_polls);
 }
 
-// Configuration: one 512-thread CTA per SM, 16 items per thread (8192-element
-// tiles). Large tiles keep the tile dispatch rate low, which keeps the
-// look-back shallow (its depth is about dispatch rate x look-back latency).
-// Counters are 32-bit up to 256 digits and 16-bit up to 2048 digits.
-struct OnesweepCfg {
-  int threads, k;
-  size_t cnt_bytes;
+// The same pass with the tile brought into shared memory by bulk copies (TMA,
+// cp.async.bulk completing on an mbarrier) instead of register loads, for up
+// to 256 digits. Elements do not occupy registers during the ranking, so a CTA
+// can run more warps; the input buffer and the staging buffer are separate, so
+// the next tile's copy is issued as soon as this tile has been read out of the
+// input buffer and overlaps all of this tile's ranking, look-back and stores.
+// Shared memory: input E x 16 B, stage E x 16 B, counters 256 x (W+1) x 4 B.
+template <int THREADS, int K, int BITS>
+__global__ void __launch_bounds__(THREADS, 1)
+    k_onesweep_tma(Elem* __restrict__ X, Elem* __restrict__ Y, uint32_t n, int bits_rt, int pass,
+                   int digit, const uint32_t* __restrict__ gstart, uint64_t* __restrict__ ring,
+                   uint32_t* __restrict__ done, uint32_t ring_tiles, Ctrl* ctrl) {
+  constexpr int W = THREADS / 32;
+  constexpr int WP = W + 1;
+  constexpr uint32_t E = THREADS * K;
+  constexpr uint32_t kSentinel = 0xffffffffu;
+  constexpr uint32_t kChunk = 32768;  // bytes per bulk copy instruction
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ __align__(8) uint64_t s_bar;
+  __shared__ uint32_t s_tile, s_next, s_err;
+  __shared__ uint32_t s_wt[33];
+
+  if (pass_skipped(ctrl, pass)) return;
+  const int bits = BITS > 0 ? BITS : bits_rt;
+  const uint32_t nbins = 1u << bits, mask = nbins - 1u;
+  const int shift = bits * digit;
+  Elem* in = reinterpret_cast<Elem*>(smem);                           // [E] tile as loaded
+  Elem* stage = in + E;                                               // [E] tile in digit order
+  uint32_t* wcnt = reinterpret_cast<uint32_t*>(stage + E);           // [256][WP]
+  uint32_t* base = wcnt + 256 * WP;                                   // [256]
+  uint32_t* tcount = base + 256;                                      // [256]
+
+  const uint32_t par = ctrl->parity[pass];
+  const Elem* __restrict__ src = par ? Y : X;
+  Elem* __restrict__ dst = par ? X : Y;
+  const uint32_t num_tiles = (n + E - 1) / E;
+  const uint32_t warp = threadIdx.x >> 5, lane = lane_id();
+  const uint32_t lt = lanemask_lt();
+  const uint32_t bar = smem_u32(&s_bar);
+
+  // thread 0 only: the bulk copy of tile tt into `in`
+  auto issue_load = [&](uint32_t tt) {
+    const uint32_t len = min(E, n - tt * E);
+    const uint32_t bytes = len * (uint32_t)sizeof(Elem);
+    const char* g = reinterpret_cast<const char*>(src + (size_t)tt * E);
+    fence_proxy_async_smem();
+    mbar_arrive_expect_tx(bar, bytes);
+    for (uint32_t off = 0; off < bytes; off += kChunk)
+      bulk_g2s(smem_u32(in) + off, g + off, min(kChunk, bytes - off), bar);
+  };
+
+  if (threadIdx.x == 0) {
+    mbar_init(bar, 1);
+    fence_mbar_init();
+    s_tile = atomicAdd(&ctrl->ticket[pass], 1u);
+    if (s_tile < num_tiles) issue_load(s_tile);
+  }
+  __syncthreads();
+  uint32_t t = s_tile;
+  uint32_t phase = 0;
+  uint32_t lb_steps = 0, lb_polls = 0;
+  bool copy_pending = t < num_tiles;
+
+  while (t < num_tiles) {
+    const uint32_t tile_len = min(E, n - t * E);
+    const bool full = tile_len == E;
+
+    // 1. wait for this tile's bytes, read the thread's items (warp-striped:
+    //    item k of lane l in warp w is element w*32*K + k*32 + l)
+    const bool arrived = mbar_wait_bounded(bar, phase);
+    if (__syncthreads_or(!arrived)) {
+      record_error(ctrl, kStatusTimeout, kWhereLookback);
+      break;
+    }
+    copy_pending = false;
+    phase ^= 1u;
+    Elem v[K];
+    uint32_t d[K];
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+      const uint32_t s = warp * 32u * K + (uint32_t)k * 32u + lane;
+      if (full || s < tile_len) {
+        v[k] = lds_elem(in + s);
+        d[k] = digit_of(v[k].key, shift, mask);
+      } else {
+        d[k] = kSentinel;
+      }
+    }
+    for (uint32_t i = threadIdx.x; i < 256u * WP; i += THREADS) wcnt[i] = 0u;
+    if (threadIdx.x == 0) {
+      s_err = 0u;
+      s_next = atomicAdd(&ctrl->ticket[pass], 1u);
+    }
+    __syncthreads();
+    const uint32_t t_next = s_next;
+    // the input buffer has been read: start copying the next tile into it
+    if (threadIdx.x == 0 && t_next < num_tiles) issue_load(t_next);
+    copy_pending = t_next < num_tiles;
+
+    // 2. stable rank inside each warp
+    uint32_t r[K];
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+      const bool valid = full || d[k] != kSentinel;
+      const uint32_t peers = (BITS > 0 && full) ? warp_peers_fixed<(BITS > 0 ? BITS : 1)>(d[k])
+                                                : warp_peers(d[k], bits, valid);
+      uint32_t* cp = &wcnt[(valid ? d[k] : 0u) * WP + warp];
+      const uint32_t c = valid ? *cp : 0u;
+      r[k] = c + __popc(peers & lt);
+      __syncwarp();
+      if (valid && lane == (uint32_t)(__ffs(peers) - 1)) *cp = c + __popc(peers);
+      __syncwarp();
+    }
+    __syncthreads();
+
+    // 3. publish the tile's digit counts (after making sure the ring slot's
+    //    previous tile has no readers left)
+    const uint32_t slot = t % ring_tiles;
+    const uint32_t tag = ring_tag(pass, t);
+    bool timed_out = false;
+    if (t >= ring_tiles) {
+      const uint32_t x = t - ring_tiles;
+      for (uint32_t j = 1 + threadIdx.x; j <= gridDim.x; j += THREADS) {
+        const uint32_t y = x + j;
+        if (y >= t) break;
+        const uint32_t want = ring_tag(pass, y);
+        uint32_t ns = 8, it = 0;
+        while (ld_acquire_u32(done + (y % ring_tiles)) < want) {
+          if (++it >= kSpinLimit || ((it & 63u) == 0u && error_raised(ctrl))) {
+            record_error(ctrl, kStatusTimeout, kWhereRingReuse);
+            timed_out = true;
+            break;
+          }
+          __nanosleep(ns);
+          if (ns < 256) ns <<= 1;
+        }
+        if (timed_out) break;
+      }
+      __syncthreads();
+    }
+    uint64_t* my = ring + (size_t)slot * nbins;
+    for (uint32_t b = threadIdx.x; b < nbins; b += THREADS) {
+      uint32_t c = 0;
+#pragma unroll
+      for (int w = 0; w < W; w++) c += wcnt[b * WP + w];
+      tcount[b] = c;
+      st_relaxed_u64(my + b, pack_status(t == 0 ? kFlagIncl : kFlagAgg, tag, c));
+    }
+
+    // 4. exclusive scan of the counters in [digit][warp] order
+    {
+      const uint32_t entries = nbins * W;
+      const uint32_t per = (entries + THREADS - 1) / THREADS;
+      const uint32_t lo = min(threadIdx.x * per, entries), hi = min(lo + per, entries);
+      uint32_t sum = 0;
+      for (uint32_t i = lo; i < hi; i++) sum += wcnt[(i / W) * WP + i % W];
+      uint32_t tot;
+      uint32_t ex = block_exclusive_scan(sum, s_wt, &tot);
+      for (uint32_t i = lo; i < hi; i++) {
+        uint32_t* p = &wcnt[(i / W) * WP + i % W];
+        const uint32_t c = *p;
+        *p = ex;
+        ex += c;
+      }
+    }
+    __syncthreads();
+    for (uint32_t b = threadIdx.x; b < nbins; b += THREADS) base[b] = wcnt[b * WP];
+
+    // 5. stage the tile in digit order
+#pragma unroll
+    for (int k = 0; k < K; k++)
+      if (full || d[k] != kSentinel) stage[r[k] + wcnt[d[k] * WP + warp]] = v[k];
+    __syncthreads();  // tile starts in base[] are read by the look-back threads
+
+    // 6. decoupled look-back per digit
+    for (uint32_t b = threadIdx.x; b < nbins; b += THREADS) {
+      uint32_t excl = 0;
+      if (t > 0) {
+        excl = lookback_digit(ring, ring_tiles, nbins, b, pass, t, ctrl, &timed_out, &lb_steps,
+                              &lb_polls);
+        st_relaxed_u64(my + b, pack_status(kFlagIncl, tag, excl + tcount[b]));
+      }
+      base[b] = gstart[b] + excl - base[b];  // dst = base[digit] + sorted position
+    }
+    if (timed_out) s_err = 1u;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      __threadfence();
+      st_release_u32(done + slot, tag);
+    }
+
+    // 7. write runs of equal digits with coalesced 16-byte stores
+    if (!s_err) {
+      if (full) {
+#pragma unroll 4
+        for (int k = 0; k < K; k++) {
+          const uint32_t pos = threadIdx.x + (uint32_t)k * THREADS;
+          const Elem e = stage[pos];
+          const uint32_t o = base[digit_of(e.key, shift, mask)] + pos;
+          if (o < n) store_elem(dst + o, e);
+        }
+      } else {
+        for (uint32_t pos = threadIdx.x; pos < tile_len; pos += THREADS) {
+          const Elem e = stage[pos];
+          const uint32_t o = base[digit_of(e.key, shift, mask)] + pos;
+          if (o < n) store_elem(dst + o, e);
+        }
+      }
+    }
+    __syncthreads();
+    t = t_next;
+  }
+  if (copy_pending && threadIdx.x == 0) {
+    // leaving early after an error: let the copy in flight land first
+    mbar_wait_bounded(bar, phase);
+  }
+  if (lb_steps) atomicAdd(&ctrl->lookback_steps, lb_steps);
+  if (lb_polls) atomicAdd(&ctrl->lookback_polls, lb_polls);
+}
+
+// Configurations (CTA shape). Large tiles keep the tile dispatch rate low,
+// which keeps the look-back shallow (its depth is about dispatch rate x
+// look-back latency); more warps per SM hide barriers and latencies.
+// Default (0): the register kernel, 512 threads x 16 items (8192-element
+// tiles, one CTA per SM), 32-bit counters up to 256 digits, 16-bit above.
+// LSB_ONESWEEP_VARIANT selects another shape (a tuning knob; measured on
+// GB300 at 2^30 elements, 8-bit digits, per pass: 0 -> 12.1 ms, 2 -> 15.5 ms,
+// 1 -> 15.8 ms, 3 -> 18.4 ms):
+//  1: bulk-copy kernel 768 x 8 (6144-element tiles, 24 warps) up to 256 digits;
+//  2: register kernel 256 x 16, two CTAs per SM;
+//  3: bulk-copy kernel 1024 x 4 (4096-element tiles, 32 warps) up to 256 digits.
+using OnesweepKernel = void (*)(Elem*, Elem*, uint32_t, int, int, int, const uint32_t*, uint64_t*,
+                                uint32_t*, uint32_t, Ctrl*);
+struct OnesweepChoice {
+  OnesweepKernel kern;
+  int threads;
+  uint32_t tile;
+  size_t smem;
 };
-static OnesweepCfg onesweep_cfg(int bits) {
-  return bits <= 8 ? OnesweepCfg{512, 16, 4} : OnesweepCfg{512, 16, 2};
-}
-#define LSB_ONESWEEP_SMALL k_onesweep<512, 16, 1, uint32_t>
-#define LSB_ONESWEEP_LARGE k_onesweep<512, 16, 1, uint16_t>
 
-uint32_t onesweep_tile_elems(int bits) {
-  const OnesweepCfg c = onesweep_cfg(bits);
-  return (uint32_t)(c.threads * c.k);
+static int onesweep_variant() {
+  const char* e = std::getenv("LSB_ONESWEEP_VARIANT");
+  const int v = e ? std::atoi(e) : 0;
+  return (v >= 0 && v <= 3) ? v : 0;
 }
 
-static size_t onesweep_smem(int bits) {
-  const OnesweepCfg c = onesweep_cfg(bits);
-  const size_t nbins = (size_t)1 << bits;
-  const size_t E = (size_t)c.threads * c.k;
-  return std::max(E * sizeof(Elem), nbins * (c.threads / 32 + 1) * c.cnt_bytes) + 2u * nbins * 4u;
+static size_t reg_kernel_smem(int bits, int threads, int k) {
+  const size_t nbins = (size_t)1 << bits, E = (size_t)threads * k;
+  const size_t cnt_bytes = bits <= 8 ? 4u : 2u;
+  return std::max(E * sizeof(Elem), nbins * (threads / 32 + 1) * cnt_bytes) + 2u * nbins * 4u;
+}
+static size_t tma_kernel_smem(int threads, int k) {
+  const size_t E = (size_t)threads * k;
+  return 2u * E * sizeof(Elem) + (256u * (threads / 32 + 1) + 512u) * 4u;
 }
 
-template <typename Kern>
-static uint32_t grid_for(Kern kern, int threads, uint32_t tile, size_t smem, const DeviceInfo& dev,
-                         uint32_t n) {
-  cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  int per_sm = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem);
-  per_sm = std::max(per_sm, 1);
-  const uint32_t tiles = (n + tile - 1) / tile;
-  return std::max<uint32_t>(1, std::min<uint32_t>(tiles, (uint32_t)(dev.sm_count * per_sm)));
+static OnesweepChoice onesweep_choice(int bits) {
+  const int v = onesweep_variant();
+  if (bits <= 8 && (v == 1 || v == 3)) {
+    if (v == 3)
+      return {bits == 8 ? k_onesweep_tma<1024, 4, 8> : k_onesweep_tma<1024, 4, 0>, 1024, 4096,
+              tma_kernel_smem(1024, 4)};
+    return {bits == 8 ? k_onesweep_tma<768, 8, 8> : k_onesweep_tma<768, 8, 0>, 768, 6144,
+            tma_kernel_smem(768, 8)};
+  }
+  if (v == 2) {
+    OnesweepKernel k = bits == 8    ? k_onesweep<256, 16, 2, uint32_t, 8>
+                       : bits == 11 ? k_onesweep<256, 16, 2, uint16_t, 11>
+                       : bits <= 8  ? k_onesweep<256, 16, 2, uint32_t, 0>
+                                    : k_onesweep<256, 16, 2, uint16_t, 0>;
+    return {k, 256, 4096, reg_kernel_smem(bits, 256, 16)};
+  }
+  OnesweepKernel k = bits == 8    ? k_onesweep<512, 16, 1, uint32_t, 8>
+                     : bits == 11 ? k_onesweep<512, 16, 1, uint16_t, 11>
+                     : bits <= 8  ? k_onesweep<512, 16, 1, uint32_t, 0>
+                                  : k_onesweep<512, 16, 1, uint16_t, 0>;
+  return {k, 512, 8192, reg_kernel_smem(bits, 512, 16)};
 }
+
+uint32_t onesweep_tile_elems(int bits) { return onesweep_choice(bits).tile; }
 
 uint32_t onesweep_grid(int bits, const DeviceInfo& dev, uint32_t n) {
-  const size_t smem = onesweep_smem(bits);
-  const uint32_t tile = onesweep_tile_elems(bits);
-  return bits <= 8 ? grid_for(LSB_ONESWEEP_SMALL, 512, tile, smem, dev, n)
-                   : grid_for(LSB_ONESWEEP_LARGE, 512, tile, smem, dev, n);
+  const OnesweepChoice c = onesweep_choice(bits);
+  cudaFuncSetAttribute(c.kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)c.smem);
+  int per_sm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, c.kern, c.threads, c.smem);
+  per_sm = std::max(per_sm, 1);
+  const uint32_t tiles = (n + c.tile - 1) / c.tile;
+  return std::max<uint32_t>(1, std::min<uint32_t>(tiles, (uint32_t)(dev.sm_count * per_sm)));
 }
 
 // ---------------------------------------------------------------------------
@@ -530,19 +814,14 @@ int onesweep_run(Elem* X, Elem* Y, int first_digit, int target_parity, unsigned 
                                        L.api_bits, L.sub, ctrl);
   }
   if (cudaPeekAtLastError() != cudaSuccess) return 5;
-  const size_t smem = onesweep_smem(L.bits);
+  const OnesweepChoice c = onesweep_choice(L.bits);
   for (int p = 0; p < L.num_digits; p++) {
     // p: index among this call's passes (parity, ticket, skip bit, ring tags);
     // first_digit + p: the digit of the key being sorted by
     const uint32_t* gs = gstart + (size_t)p * nbins;
     ProfScope prof("onesweep_scatter", st);
-    if (L.bits <= 8) {
-      LSB_ONESWEEP_SMALL<<<L.grid, 512, smem, st>>>(X, Y, L.n, L.bits, p, first_digit + p, gs,
-                                                    ring, done, L.ring_tiles, ctrl);
-    } else {
-      LSB_ONESWEEP_LARGE<<<L.grid, 512, smem, st>>>(X, Y, L.n, L.bits, p, first_digit + p, gs,
-                                                    ring, done, L.ring_tiles, ctrl);
-    }
+    c.kern<<<L.grid, c.threads, c.smem, st>>>(X, Y, L.n, L.bits, p, first_digit + p, gs, ring,
+                                              done, L.ring_tiles, ctrl);
     if (cudaPeekAtLastError() != cudaSuccess) return 5;
   }
   return final_copy(X, Y, L.n, L.num_digits, target_parity, ctrl, st);
