@@ -49,6 +49,16 @@ struct Ctrl {
 static_assert(sizeof(Ctrl) <= 1024, "control block must fit its 1 KiB slot");
 constexpr size_t kCtrlBytes = 1024;
 
+// A batch of independent arrays sorted together (null tile_seg: one array).
+struct SegDesc {
+  const uint32_t* tile_seg = nullptr;   // [tiles] segment of each tile
+  const uint32_t* seg_tile0 = nullptr;  // [nseg] first tile of each segment
+  const int64_t* seg_off = nullptr;     // [nseg + 1] element offsets of the segments
+  const uint32_t* seg_gstart = nullptr; // [nseg][passes][2^b] exclusive digit starts
+  const uint32_t* num_tiles = nullptr;  // tiles in the batch (device word)
+  int num_passes = 0;
+};
+
 struct __align__(16) Elem {
   uint64_t key;
   uint64_t val;

@@ -70,6 +70,12 @@ int onesweep_run(Elem* X, Elem* Y, int first_digit, int target_parity, unsigned 
 int task_run(Elem* X, Elem* Y, int first_digit, int target_parity, unsigned char* ws,
              const Layout& L, cudaStream_t st);
 uint32_t onesweep_tile_elems(int bits);
+// explicit kernel shape (variant 0: 512 threads x 16, 1 CTA/SM; 2: 256 x 16, 2 CTAs/SM)
+uint32_t onesweep_tile_elems_v(int bits, int variant);
+uint32_t onesweep_grid_v(int bits, int variant, const DeviceInfo& dev, uint32_t tiles);
+int onesweep_launch_v(int bits, int variant, uint32_t grid, Elem* X, Elem* Y, uint32_t n, int pass,
+                      int digit, const uint32_t* gstart, uint64_t* ring, uint32_t* done,
+                      uint32_t ring_tiles, Ctrl* ctrl, const SegDesc& seg, cudaStream_t st);
 uint32_t onesweep_grid(int bits, const DeviceInfo& dev, uint32_t n);
 uint32_t task_count(const DeviceInfo& dev, uint32_t n);
 

@@ -266,7 +266,7 @@ template <int THREADS, int K, int MINB, typename CNT, int BITS>
 __global__ void __launch_bounds__(THREADS, MINB)
     k_onesweep(Elem* __restrict__ X, Elem* __restrict__ Y, uint32_t n, int bits_rt, int pass,
                int digit, const uint32_t* __restrict__ gstart, uint64_t* __restrict__ ring,
-               uint32_t* __restrict__ done, uint32_t ring_tiles, Ctrl* ctrl) {
+               uint32_t* __restrict__ done, uint32_t ring_tiles, Ctrl* ctrl, SegDesc seg) {
   constexpr int W = THREADS / 32;
   constexpr int WP = W + 1;  // padded row: the lanes of a warp hit different banks
   constexpr uint32_t E = THREADS * K;
@@ -289,17 +289,47 @@ __global__ void __launch_bounds__(THREADS, MINB)
   const uint32_t par = ctrl->parity[pass];
   const Elem* __restrict__ src = par ? Y : X;
   Elem* __restrict__ dst = par ? X : Y;
-  const uint32_t num_tiles = (n + E - 1) / E;
+  const bool segmented = seg.tile_seg != nullptr;
+  const uint32_t num_tiles = segmented ? *seg.num_tiles : (n + E - 1) / E;
   const uint32_t warp = threadIdx.x >> 5, lane = lane_id();
   const uint32_t lt = lanemask_lt();
+
+  // where tile t lives: one array, or tile j of segment s of a batch (the
+  // first tile of every segment starts its own look-back chain)
+  struct TileInfo {
+    uint32_t begin, len, seg_base;
+    bool first;
+    const uint32_t* gs;
+  };
+  auto tile_info = [&](uint32_t t) {
+    TileInfo ti;
+    if (!segmented) {
+      ti.begin = t * E;
+      ti.len = min(E, n - ti.begin);
+      ti.seg_base = 0;
+      ti.first = t == 0;
+      ti.gs = gstart;
+    } else {
+      const uint32_t sg = seg.tile_seg[t];
+      const uint32_t j = t - seg.seg_tile0[sg];
+      const uint32_t sb = (uint32_t)seg.seg_off[sg], se = (uint32_t)seg.seg_off[sg + 1];
+      ti.begin = sb + j * E;
+      ti.len = min(E, se - ti.begin);
+      ti.seg_base = sb;
+      ti.first = j == 0;
+      ti.gs = seg.seg_gstart + ((size_t)sg * seg.num_passes + pass) * nbins;
+    }
+    return ti;
+  };
 
   Elem v[K];
   uint32_t d[K];
   // loads tile `t` warp-striped: item k of lane l in warp w is tile element
   // w*32*K + k*32 + l (coalesced 512-byte warp loads)
   auto load_tile = [&](uint32_t t) {
-    const uint32_t tile_begin = t * E;
-    const uint32_t len = min(E, n - tile_begin);
+    const TileInfo ti = tile_info(t);
+    const uint32_t tile_begin = ti.begin;
+    const uint32_t len = ti.len;
     const Elem* p = src + tile_begin + warp * 32u * K + lane;
     if (len == E) {
 #pragma unroll
@@ -327,7 +357,8 @@ __global__ void __launch_bounds__(THREADS, MINB)
   uint32_t lb_steps = 0, lb_polls = 0;
 
   while (t < num_tiles) {
-    const uint32_t tile_len = min(E, n - t * E);
+    const TileInfo ti = tile_info(t);
+    const uint32_t tile_len = ti.len;
     if (threadIdx.x == 0) s_err = 0u;
     for (uint32_t i = threadIdx.x; i < nbins * WP; i += THREADS) wcnt[i] = 0;
     __syncthreads();
@@ -396,7 +427,7 @@ __global__ void __launch_bounds__(THREADS, MINB)
 #pragma unroll
       for (int w = 0; w < W; w++) c += wcnt[b * WP + w];
       tcount[b] = c;
-      st_relaxed_u64(my + b, pack_status(t == 0 ? kFlagIncl : kFlagAgg, tag, c));
+      st_relaxed_u64(my + b, pack_status(ti.first ? kFlagIncl : kFlagAgg, tag, c));
     }
 
     // 3. exclusive scan of the counters in [digit][warp] order: the start of
@@ -436,12 +467,12 @@ __global__ void __launch_bounds__(THREADS, MINB)
     // 5. decoupled look-back per digit
     for (uint32_t b = threadIdx.x; b < nbins; b += THREADS) {
       uint32_t excl = 0;
-      if (t > 0) {
+      if (!ti.first) {
         excl = lookback_digit(ring, ring_tiles, nbins, b, pass, t, ctrl, &timed_out, &lb_steps,
                               &lb_polls);
         st_relaxed_u64(my + b, pack_status(kFlagIncl, tag, excl + tcount[b]));
       }
-      base[b] = gstart[b] + excl - base[b];  // dst = base[digit] + sorted position
+      base[b] = ti.seg_base + ti.gs[b] + excl - base[b];  // dst = base[digit] + sorted position
     }
     if (timed_out) s_err = 1u;
     __syncthreads();
@@ -486,7 +517,7 @@ template <int THREADS, int K, int BITS>
 __global__ void __launch_bounds__(THREADS, 1)
     k_onesweep_tma(Elem* __restrict__ X, Elem* __restrict__ Y, uint32_t n, int bits_rt, int pass,
                    int digit, const uint32_t* __restrict__ gstart, uint64_t* __restrict__ ring,
-                   uint32_t* __restrict__ done, uint32_t ring_tiles, Ctrl* ctrl) {
+                   uint32_t* __restrict__ done, uint32_t ring_tiles, Ctrl* ctrl, SegDesc) {
   constexpr int W = THREADS / 32;
   constexpr int WP = W + 1;
   constexpr uint32_t E = THREADS * K;
@@ -707,7 +738,7 @@ __global__ void __launch_bounds__(THREADS, 1)
 //  2: register kernel 256 x 16, two CTAs per SM;
 //  3: bulk-copy kernel 1024 x 4 (4096-element tiles, 32 warps) up to 256 digits.
 using OnesweepKernel = void (*)(Elem*, Elem*, uint32_t, int, int, int, const uint32_t*, uint64_t*,
-                                uint32_t*, uint32_t, Ctrl*);
+                                uint32_t*, uint32_t, Ctrl*, SegDesc);
 struct OnesweepChoice {
   OnesweepKernel kern;
   int threads;
@@ -731,8 +762,7 @@ static size_t tma_kernel_smem(int threads, int k) {
   return 2u * E * sizeof(Elem) + (256u * (threads / 32 + 1) + 512u) * 4u;
 }
 
-static OnesweepChoice onesweep_choice(int bits) {
-  const int v = onesweep_variant();
+static OnesweepChoice onesweep_choice(int bits, int v) {
   if (bits <= 8 && (v == 1 || v == 3)) {
     if (v == 3)
       return {bits == 8 ? k_onesweep_tma<1024, 4, 8> : k_onesweep_tma<1024, 4, 0>, 1024, 4096,
@@ -754,7 +784,32 @@ static OnesweepChoice onesweep_choice(int bits) {
   return {k, 512, 8192, reg_kernel_smem(bits, 512, 16)};
 }
 
+static OnesweepChoice onesweep_choice(int bits) { return onesweep_choice(bits, onesweep_variant()); }
+
 uint32_t onesweep_tile_elems(int bits) { return onesweep_choice(bits).tile; }
+
+uint32_t onesweep_tile_elems_v(int bits, int variant) {
+  return onesweep_choice(bits, variant).tile;
+}
+
+uint32_t onesweep_grid_v(int bits, int variant, const DeviceInfo& dev, uint32_t tiles) {
+  const OnesweepChoice c = onesweep_choice(bits, variant);
+  cudaFuncSetAttribute(c.kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)c.smem);
+  int per_sm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, c.kern, c.threads, c.smem);
+  per_sm = std::max(per_sm, 1);
+  return std::max<uint32_t>(1, std::min<uint32_t>(tiles, (uint32_t)(dev.sm_count * per_sm)));
+}
+
+int onesweep_launch_v(int bits, int variant, uint32_t grid, Elem* X, Elem* Y, uint32_t n, int pass,
+                      int digit, const uint32_t* gstart, uint64_t* ring, uint32_t* done,
+                      uint32_t ring_tiles, Ctrl* ctrl, const SegDesc& seg, cudaStream_t st) {
+  const OnesweepChoice c = onesweep_choice(bits, variant);
+  ProfScope prof("onesweep_scatter", st);
+  c.kern<<<grid, c.threads, c.smem, st>>>(X, Y, n, bits, pass, digit, gstart, ring, done, ring_tiles,
+                                          ctrl, seg);
+  return cudaPeekAtLastError() == cudaSuccess ? 0 : 5;
+}
 
 uint32_t onesweep_grid(int bits, const DeviceInfo& dev, uint32_t n) {
   const OnesweepChoice c = onesweep_choice(bits);
@@ -821,7 +876,7 @@ int onesweep_run(Elem* X, Elem* Y, int first_digit, int target_parity, unsigned 
     const uint32_t* gs = gstart + (size_t)p * nbins;
     ProfScope prof("onesweep_scatter", st);
     c.kern<<<L.grid, c.threads, c.smem, st>>>(X, Y, L.n, L.bits, p, first_digit + p, gs, ring,
-                                              done, L.ring_tiles, ctrl);
+                                              done, L.ring_tiles, ctrl, SegDesc{});
     if (cudaPeekAtLastError() != cudaSuccess) return 5;
   }
   return final_copy(X, Y, L.n, L.num_digits, target_parity, ctrl, st);

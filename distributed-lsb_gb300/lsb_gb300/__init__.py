@@ -50,6 +50,13 @@ SIGNATURES = {
     "lsb_generate": (ctypes.c_int, [_P, _I64, ctypes.c_int, ctypes.c_uint64, _P]),
     "lsb_verify": (ctypes.c_int, [_P, _P, _I64, ctypes.POINTER(ctypes.c_uint64), _P]),
     "lsb_sort_pairs_noalloc": (ctypes.c_int, [_P, _P, _I64, ctypes.c_int, _P]),
+    "lsb_segmented_workspace_bytes": (ctypes.c_int, [_I64, _I64, ctypes.c_int, ctypes.POINTER(ctypes.c_size_t)]),
+    "lsb_sort_segmented": (ctypes.c_int, [_P, _P, _I64, _P, _I64, _P, _P, ctypes.c_size_t, _P]),
+    "lsb_tune_segmented": (ctypes.c_int, [_P, _I64, _P, _P]),
+    "lsb_graph_capture_segmented": (ctypes.c_int, [_P, _P, _I64, _P, _I64, _P, _P, ctypes.c_size_t,
+                                                   ctypes.POINTER(ctypes.c_void_p)]),
+    "lsb_graph_launch": (ctypes.c_int, [_P, _P]),
+    "lsb_graph_destroy": (ctypes.c_int, [_P]),
     "lsb_profile_enable": (ctypes.c_int, [ctypes.c_int]),
     "lsb_profile_read": (ctypes.c_int, [_P, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]),
 }
@@ -59,6 +66,12 @@ class KernelTime(ctypes.Structure):
     """lsb_kernel_time_t"""
 
     _fields_ = [("name", ctypes.c_char * 40), ("launches", ctypes.c_int64), ("total_ms", ctypes.c_double)]
+
+
+class Tuning(ctypes.Structure):
+    """lsb_tuning_t"""
+
+    _fields_ = [("digit_bits", ctypes.c_int32), ("variant", ctypes.c_int32), ("reserved", ctypes.c_int32 * 2)]
 
 
 class Stats(ctypes.Structure):
@@ -196,6 +209,69 @@ def generate(n: int, dist: int = DIST_UNIFORM, seed: int = 1, out=None, device=N
         out = torch.empty((n, 2), dtype=torch.int64, device=device or "cuda")
     _check(load().lsb_generate(_ptr(out), n, dist, seed, _stream_ptr(stream)), "lsb_generate")
     return out
+
+
+def segmented_workspace_bytes(n_total: int, nseg: int, digit_bits: int = 16) -> int:
+    out = ctypes.c_size_t(0)
+    _check(load().lsb_segmented_workspace_bytes(n_total, nseg, digit_bits, ctypes.byref(out)),
+           "lsb_segmented_workspace_bytes")
+    return out.value
+
+
+def alloc_segmented_workspace(n_total: int, nseg: int, digit_bits: int = 16, device=None):
+    import torch
+
+    nbytes = segmented_workspace_bytes(n_total, nseg, digit_bits)
+    return torch.empty(max(nbytes, 256), dtype=torch.uint8, device=device or "cuda")
+
+
+def tune_segmented(offsets_host, stream=None) -> Tuning:
+    """The autotuner: best (digit width, kernel shape) for this size mix."""
+    import numpy as np
+
+    off = np.ascontiguousarray(offsets_host, dtype=np.int64)
+    t = Tuning()
+    _check(load().lsb_tune_segmented(ctypes.c_void_p(off.ctypes.data), off.shape[0] - 1, ctypes.byref(t),
+                                     _stream_ptr(stream)), "lsb_tune_segmented")
+    return t
+
+
+def sort_segmented(a, b, offsets, tuning: Tuning | None = None, workspace=None, stream=None) -> None:
+    """Sorts every segment a[offsets[s]:offsets[s+1]] in place (offsets: int64
+    CUDA tensor of nseg + 1 entries)."""
+    ws = _ptr(workspace) if workspace is not None else ctypes.c_void_p(0)
+    wsb = workspace.numel() if workspace is not None else 0
+    tp = ctypes.byref(tuning) if tuning is not None else None
+    _check(load().lsb_sort_segmented(_ptr(a), _ptr(b), a.shape[0], _ptr(offsets), offsets.shape[0] - 1, tp,
+                                     ws, wsb, _stream_ptr(stream)), "lsb_sort_segmented")
+
+
+class SegmentedGraph:
+    """The batch sort captured into a CUDA graph (lsb_graph_capture_segmented)."""
+
+    def __init__(self, a, b, offsets, tuning: Tuning | None, workspace):
+        self._keep = (a, b, offsets, workspace)
+        h = ctypes.c_void_p(0)
+        tp = ctypes.byref(tuning) if tuning is not None else None
+        _check(load().lsb_graph_capture_segmented(_ptr(a), _ptr(b), a.shape[0], _ptr(offsets),
+                                                  offsets.shape[0] - 1, tp, _ptr(workspace),
+                                                  workspace.numel(), ctypes.byref(h)),
+               "lsb_graph_capture_segmented")
+        self.handle = h
+
+    def launch(self, stream=None) -> None:
+        _check(load().lsb_graph_launch(self.handle, _stream_ptr(stream)), "lsb_graph_launch")
+
+    def close(self) -> None:
+        if self.handle:
+            load().lsb_graph_destroy(self.handle)
+            self.handle = ctypes.c_void_p(0)
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def profile_enable(on: bool = True) -> None:

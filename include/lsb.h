@@ -152,6 +152,50 @@ int lsb_generate(lsb_elem_t* d_out, int64_t n, int dist, uint64_t seed, void* st
 int lsb_verify(const lsb_elem_t* d_in, const lsb_elem_t* d_out, int64_t n, uint64_t* h_mismatches,
                void* stream);
 
+/* ---- batches of independent arrays (segmented sort) ----------------------
+ * The reference sorts one array per program run (mySort,
+ * mpi/mpi_lsbsort.cpp:592-597); sorting many arrays means calling it once per
+ * array. These entry points sort a batch of arrays stored back to back in one
+ * buffer in the same launches. Segment s is d_a[off[s] .. off[s+1]) with
+ * off[0] = 0 and off[nseg] = n_total (device array of nseg + 1 int64). Each
+ * segment ends up sorted exactly as lsb_sort_pairs would sort it alone.
+ * Digit widths 1..11, 12, 14 and 16 (wide even widths run as two half-width
+ * sub-passes per digit). */
+typedef struct lsb_tuning {
+  int32_t digit_bits; /* digit width of the passes (result identical for all)  */
+  int32_t variant;    /* kernel shape: 0 = 8192-element tiles, 1 CTA per SM;
+                         2 = 4096-element tiles, 2 CTAs per SM                 */
+  int32_t reserved[2];
+} lsb_tuning_t;
+
+/* Workspace for lsb_sort_segmented / lsb_graph_capture_segmented (any variant). */
+int lsb_segmented_workspace_bytes(int64_t n_total, int64_t nseg, int digit_bits, size_t* bytes);
+
+/* Sorts every segment of d_a in place (d_b scratch, same length). opt_tuning
+ * NULL = 8-bit digits, variant 0. Workspace rules as for lsb_sort_pairs.
+ * Stream-ordered and free of host synchronisation when a workspace is given,
+ * so it can be captured in a CUDA graph. */
+int lsb_sort_segmented(lsb_elem_t* d_a, lsb_elem_t* d_b, int64_t n_total,
+                       const int64_t* d_seg_offsets, int64_t nseg, const lsb_tuning_t* opt_tuning,
+                       void* d_workspace, size_t workspace_bytes, void* stream);
+
+/* Autotuner: times every candidate configuration (digit width 8 or 11, kernel
+ * shape 0 or 2) on a sample batch with the same segment sizes as
+ * h_seg_offsets (host array, nseg + 1 entries; random keys, at most ~2^26
+ * elements) and returns the fastest. Results are cached per size class (log2
+ * of the total and of the mean segment size). Blocking; allocates. */
+int lsb_tune_segmented(const int64_t* h_seg_offsets, int64_t nseg, lsb_tuning_t* out, void* stream);
+
+/* The whole batch sort captured once into an executable CUDA graph; every
+ * lsb_graph_launch re-sorts the same buffers (whatever they hold then). */
+typedef struct lsb_graph lsb_graph_t;
+int lsb_graph_capture_segmented(lsb_elem_t* d_a, lsb_elem_t* d_b, int64_t n_total,
+                                const int64_t* d_seg_offsets, int64_t nseg,
+                                const lsb_tuning_t* opt_tuning, void* d_workspace,
+                                size_t workspace_bytes, lsb_graph_t** out);
+int lsb_graph_launch(lsb_graph_t* graph, void* stream);
+int lsb_graph_destroy(lsb_graph_t* graph);
+
 /* Sort without any device allocation. No counterpart in the reference: it is
  * for callers that may not allocate device memory -- a host framework that
  * owns all GPU memory through its own arena, a latency-critical path that
