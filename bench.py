@@ -66,6 +66,10 @@ def args_parse(argv=None):
     p.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
     p.add_argument("--no-extra", action="store_true", help="skip the 8-bit-digit side measurement")
     p.add_argument("--cpu-sample", type=int, default=1 << 26)
+    p.add_argument("--no-segmented", action="store_true", help="skip the batched segmented leg")
+    p.add_argument("--segments", type=int, default=4096)
+    p.add_argument("--seg-steps", type=int, default=3)
+    p.add_argument("--seg-seed", type=int, default=2024)
     return p.parse_args(argv)
 
 
@@ -406,12 +410,80 @@ def gpu_arm(args, ranks: Ranks):
                       "call": "lsb_sort_pairs_host (pinned host buffer)", "sorted_check": ok}
         del h
 
+    if not args.no_segmented:
+        A = B = ws = None  # release the 2^30 buffers (32 GiB) before the batch
+        torch.cuda.empty_cache()
+        out["segmented"] = segmented_leg(args, lsb, torch, ranks)
+
     if ranks.rank == 0 and ranks.world == 1 and not args.no_cpu:
         val, times, threads = cpu_sort_rate(args.cpu_sample, 3, warmup=1, budget_s=30.0)
         out["cpu_baseline"] = {"value": round(val, 3), "unit": UNIT, "cores": threads, "kind": "port",
                                "sample": f"{args.cpu_sample} uniform elements, 16-bit digits, "
                                          f"{len(times)} timed sorts, {threads} simulated ranks"}
     return out
+
+
+def segmented_leg(args, lsb, torch, ranks) -> dict:
+    """Batched segmented sort: 4096 arrays with sizes floor(2^U(10, 22)) (seeded),
+    uniform keys, value = index; one CUDA-graph launch with the autotuned
+    configuration against a loop of lsb_sort_pairs (16-bit digits) over the
+    same arrays. Both start from the same unsorted input; outputs must match."""
+    import numpy as np
+
+    rng = np.random.default_rng(args.seg_seed)
+    sizes = np.floor(2.0 ** rng.uniform(10, 22, size=args.segments)).astype(np.int64)
+    off = np.zeros(len(sizes) + 1, dtype=np.int64)
+    off[1:] = np.cumsum(sizes)
+    total = int(off[-1])
+    stream = torch.cuda.current_stream()
+    src = lsb.generate(total, 0, seed=1000 + ranks.rank)
+    A = torch.empty_like(src)
+    B = torch.empty_like(src)
+    offs = torch.from_numpy(off).cuda()
+    tuning = lsb.tune_segmented(off)
+    ws = lsb.alloc_segmented_workspace(total, len(sizes), tuning.digit_bits)
+    graph = lsb.SegmentedGraph(A, B, offs, tuning, ws)
+
+    def timed(fn, reps, warm):
+        ms = []
+        for i in range(warm + reps):
+            A.copy_(src)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            if i >= warm:
+                ms.append(e0.elapsed_time(e1))
+        return ms
+
+    batched = timed(lambda: graph.launch(), args.seg_steps, 1)
+    batched_out = A.clone()
+    big = int(sizes.max())
+    ws1 = lsb.alloc_workspace(big, 16)
+    views = [(A[off[s]:off[s + 1]], B[off[s]:off[s + 1]]) for s in range(len(sizes)) if sizes[s] > 0]
+
+    def loop():
+        for a_s, b_s in views:
+            lsb.sort_pairs(a_s, b_s, 16, workspace=ws1[: max(256, lsb.workspace_bytes(a_s.shape[0], 16))])
+
+    looped = timed(loop, max(1, args.seg_steps - 1), 1)
+    identical = bool(torch.equal(batched_out, A))
+    graph.close()
+    bms, lms = statistics.mean(batched), statistics.mean(looped)
+    res = {
+        "segments": len(sizes), "elements": total, "size_law": "floor(2^U(10,22))",
+        "tuning": {"digit_bits": tuning.digit_bits, "variant": tuning.variant},
+        "batched_ms": round(bms, 3), "loop_ms": round(lms, 3), "speedup": round(lms / bms, 3),
+        "batched_value": round(total / (bms / 1e3) / 1e6, 3), "loop_value": round(total / (lms / 1e3) / 1e6, 3),
+        "unit": UNIT, "identical_outputs": identical,
+        "batched_p50_ms": round(statistics.median(batched), 3),
+        "batched_p99_ms": round(sorted(batched)[min(len(batched) - 1, int(0.99 * len(batched)))], 3),
+        "loop_call": "lsb_sort_pairs per array, 16-bit digits, one workspace, Python ctypes loop",
+    }
+    del A, B, src, ws, ws1, views
+    torch.cuda.empty_cache()
+    return res
 
 
 def main(argv=None):
