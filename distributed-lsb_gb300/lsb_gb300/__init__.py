@@ -57,6 +57,14 @@ SIGNATURES = {
                                                    ctypes.POINTER(ctypes.c_void_p)]),
     "lsb_graph_launch": (ctypes.c_int, [_P, _P]),
     "lsb_graph_destroy": (ctypes.c_int, [_P]),
+    "lsb_server_create": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_void_p)]),
+    "lsb_server_submit_host": (ctypes.c_int, [_P, _P, _I64, ctypes.POINTER(ctypes.c_uint64)]),
+    "lsb_server_submit_generated": (ctypes.c_int, [_P, _I64, ctypes.c_int, ctypes.c_uint64, ctypes.c_int,
+                                                   ctypes.POINTER(ctypes.c_uint64)]),
+    "lsb_server_wait": (ctypes.c_int, [_P, ctypes.c_uint64, ctypes.c_double, _P]),
+    "lsb_server_fetch": (ctypes.c_int, [_P, ctypes.c_uint64, _P, _I64]),
+    "lsb_server_stats": (ctypes.c_int, [_P, _P]),
+    "lsb_server_destroy": (ctypes.c_int, [_P]),
     "lsb_profile_enable": (ctypes.c_int, [ctypes.c_int]),
     "lsb_profile_read": (ctypes.c_int, [_P, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]),
 }
@@ -72,6 +80,32 @@ class Tuning(ctypes.Structure):
     """lsb_tuning_t"""
 
     _fields_ = [("digit_bits", ctypes.c_int32), ("variant", ctypes.c_int32), ("reserved", ctypes.c_int32 * 2)]
+
+
+class ServerConfig(ctypes.Structure):
+    """lsb_server_config_t"""
+
+    _fields_ = [("slots", ctypes.c_int32), ("digit_bits", ctypes.c_int32), ("hbm_budget_bytes", ctypes.c_int64),
+                ("batch_max_elems", ctypes.c_int64), ("batch_max_requests", ctypes.c_int32),
+                ("reserved", ctypes.c_int32)]
+
+
+class RequestInfo(ctypes.Structure):
+    """lsb_request_info_t"""
+
+    _fields_ = [("status", ctypes.c_int32), ("batch", ctypes.c_int32), ("n", ctypes.c_int64),
+                ("latency_ms", ctypes.c_double), ("queue_ms", ctypes.c_double)]
+
+
+class ServerStats(ctypes.Structure):
+    """lsb_server_stats_t"""
+
+    _fields_ = [("requests_done", ctypes.c_int64), ("elements_done", ctypes.c_int64), ("units", ctypes.c_int64),
+                ("batched_requests", ctypes.c_int64), ("peak_bytes", ctypes.c_int64),
+                ("budget_bytes", ctypes.c_int64), ("latency_p50_ms", ctypes.c_double),
+                ("latency_p99_ms", ctypes.c_double), ("service_p50_ms", ctypes.c_double),
+                ("service_p99_ms", ctypes.c_double), ("wall_ms", ctypes.c_double),
+                ("elements_per_s", ctypes.c_double)]
 
 
 class Stats(ctypes.Structure):
@@ -272,6 +306,60 @@ class SegmentedGraph:
             self.close()
         except Exception:
             pass
+
+
+class Server:
+    """The request loop (lsb_server_*): continuous batching of sort requests."""
+
+    def __init__(self, slots: int = 4, digit_bits: int = 16, hbm_budget_bytes: int = 0,
+                 batch_max_elems: int = 0, batch_max_requests: int = 0):
+        cfg = ServerConfig(slots=slots, digit_bits=digit_bits, hbm_budget_bytes=hbm_budget_bytes,
+                           batch_max_elems=batch_max_elems, batch_max_requests=batch_max_requests)
+        h = ctypes.c_void_p(0)
+        _check(load().lsb_server_create(ctypes.byref(cfg), ctypes.byref(h)), "lsb_server_create")
+        self.handle = h
+
+    def submit_generated(self, n: int, dist: int = DIST_UNIFORM, seed: int = 1, keep: bool = False) -> int:
+        rid = ctypes.c_uint64(0)
+        _check(load().lsb_server_submit_generated(self.handle, n, dist, seed, 1 if keep else 0, ctypes.byref(rid)),
+               "lsb_server_submit_generated")
+        return rid.value
+
+    def submit_host(self, array) -> int:
+        """array: numpy uint64 (n, 2) or CPU tensor; sorted in place."""
+        ptr = array.data_ptr() if hasattr(array, "data_ptr") else array.ctypes.data
+        rid = ctypes.c_uint64(0)
+        _check(load().lsb_server_submit_host(self.handle, ctypes.c_void_p(ptr), array.shape[0], ctypes.byref(rid)),
+               "lsb_server_submit_host")
+        return rid.value
+
+    def wait(self, rid: int, timeout_s: float = 600.0) -> RequestInfo:
+        info = RequestInfo()
+        _check(load().lsb_server_wait(self.handle, rid, timeout_s, ctypes.byref(info)), "lsb_server_wait")
+        return info
+
+    def fetch(self, rid: int, n: int):
+        import numpy as np
+
+        out = np.empty((n, 2), dtype=np.uint64)
+        _check(load().lsb_server_fetch(self.handle, rid, ctypes.c_void_p(out.ctypes.data), n), "lsb_server_fetch")
+        return out
+
+    def stats(self) -> ServerStats:
+        st = ServerStats()
+        _check(load().lsb_server_stats(self.handle, ctypes.byref(st)), "lsb_server_stats")
+        return st
+
+    def close(self) -> None:
+        if self.handle:
+            load().lsb_server_destroy(self.handle)
+            self.handle = ctypes.c_void_p(0)
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
 
 
 def profile_enable(on: bool = True) -> None:

@@ -196,6 +196,57 @@ int lsb_graph_capture_segmented(lsb_elem_t* d_a, lsb_elem_t* d_b, int64_t n_tota
 int lsb_graph_launch(lsb_graph_t* graph, void* stream);
 int lsb_graph_destroy(lsb_graph_t* graph);
 
+/* ---- request loop (serving) ---------------------------------------------
+ * No counterpart in the reference, which sorts one array per program run.
+ * A server owns a worker thread, `slots` CUDA streams and a memory pool.
+ * Requests are admitted in arrival order whenever a stream slot is free and
+ * their buffers (A + B + workspace) fit in the HBM budget; consecutive small
+ * requests (up to batch_max_elems elements together, batch_max_requests of
+ * them) are sorted as one segmented batch; requests admitted on different
+ * slots run concurrently. Pool memory stays resident between requests.
+ * Every request's result is exactly lsb_sort_pairs of its input alone. */
+typedef struct lsb_server_config {
+  int32_t slots;              /* concurrent streams (default 4)                     */
+  int32_t digit_bits;         /* digit width of the sorts (default 16)             */
+  int64_t hbm_budget_bytes;   /* admission budget (default 80% of free memory)     */
+  int64_t batch_max_elems;    /* requests up to this size are batched (default 2^22) */
+  int32_t batch_max_requests; /* most requests in one batch (default 4096)         */
+  int32_t reserved;
+} lsb_server_config_t;
+
+typedef struct lsb_request_info {
+  int32_t status;    /* LSB_OK or the error of this request               */
+  int32_t batch;     /* requests sorted together with it (1 = alone)      */
+  int64_t n;
+  double latency_ms; /* submit -> result ready (host clock)               */
+  double queue_ms;   /* submit -> admitted                                */
+} lsb_request_info_t;
+
+typedef struct lsb_server_stats {
+  int64_t requests_done, elements_done, units, batched_requests, peak_bytes, budget_bytes;
+  double latency_p50_ms, latency_p99_ms; /* submit -> done                   */
+  double service_p50_ms, service_p99_ms; /* admitted -> done                 */
+  double wall_ms;                        /* first submit -> last completion  */
+  double elements_per_s;
+} lsb_server_stats_t;
+
+typedef struct lsb_server lsb_server_t;
+int lsb_server_create(const lsb_server_config_t* cfg, lsb_server_t** out);
+/* Sorts h_data[0..n) in place (host memory; keep it valid until the request
+ * is done; page-locked memory copies fastest). */
+int lsb_server_submit_host(lsb_server_t* server, lsb_elem_t* h_data, int64_t n, uint64_t* id);
+/* Input generated on the device (lsb_generate(n, dist, seed)); with
+ * keep_result the sorted array stays on the device until lsb_server_fetch. */
+int lsb_server_submit_generated(lsb_server_t* server, int64_t n, int dist, uint64_t seed,
+                                int keep_result, uint64_t* id);
+/* Blocks until request `id` is done (LSB_ERR_DEVICE_TIMEOUT after timeout_s). */
+int lsb_server_wait(lsb_server_t* server, uint64_t id, double timeout_s, lsb_request_info_t* info);
+/* Copies a kept result to host memory and releases it. */
+int lsb_server_fetch(lsb_server_t* server, uint64_t id, lsb_elem_t* h_out, int64_t n);
+int lsb_server_stats(lsb_server_t* server, lsb_server_stats_t* out);
+/* Finishes every submitted request, then frees everything. */
+int lsb_server_destroy(lsb_server_t* server);
+
 /* Sort without any device allocation. No counterpart in the reference: it is
  * for callers that may not allocate device memory -- a host framework that
  * owns all GPU memory through its own arena, a latency-critical path that
