@@ -70,6 +70,10 @@ def args_parse(argv=None):
     p.add_argument("--segments", type=int, default=4096)
     p.add_argument("--seg-steps", type=int, default=3)
     p.add_argument("--seg-seed", type=int, default=2024)
+    p.add_argument("--no-serving", action="store_true", help="skip the request-loop leg")
+    p.add_argument("--requests", type=int, default=10000)
+    p.add_argument("--rate", type=float, default=400.0, help="Poisson arrival rate, requests/s")
+    p.add_argument("--serve-slots", type=int, default=4)
     return p.parse_args(argv)
 
 
@@ -415,6 +419,9 @@ def gpu_arm(args, ranks: Ranks):
         torch.cuda.empty_cache()
         out["segmented"] = segmented_leg(args, lsb, torch, ranks)
 
+    if not args.no_serving:
+        out["serving"] = serving_leg(args, lsb, torch, ranks)
+
     if ranks.rank == 0 and ranks.world == 1 and not args.no_cpu:
         val, times, threads = cpu_sort_rate(args.cpu_sample, 3, warmup=1, budget_s=30.0)
         out["cpu_baseline"] = {"value": round(val, 3), "unit": UNIT, "cores": threads, "kind": "port",
@@ -484,6 +491,44 @@ def segmented_leg(args, lsb, torch, ranks) -> dict:
     del A, B, src, ws, ws1, views
     torch.cuda.empty_cache()
     return res
+
+
+def serving_leg(args, lsb, torch, ranks) -> dict:
+    """Open-loop request stream: Poisson arrivals at args.rate, sizes
+    floor(2^U(10, 27)) elements of uniform keys (generated on the device per
+    request), 16-bit digits, through the request loop (lsb_server_*)."""
+    import numpy as np
+
+    rng = np.random.default_rng(7 + ranks.rank)
+    sizes = np.floor(2.0 ** rng.uniform(10, 27, size=args.requests)).astype(np.int64)
+    arrivals = np.cumsum(rng.exponential(1.0 / args.rate, size=args.requests))
+    with lsb.Server(slots=args.serve_slots, digit_bits=16) as srv:
+        t0 = time.perf_counter()
+        ids = []
+        for i in range(args.requests):
+            delay = t0 + arrivals[i] - time.perf_counter()
+            if delay > 0.002:
+                time.sleep(delay - 0.001)
+            while time.perf_counter() < t0 + arrivals[i]:
+                pass
+            ids.append(srv.submit_generated(int(sizes[i]), 0, 1 + i))
+        batched = 0
+        for r in ids:
+            info = srv.wait(r)
+            if info.status != 0:
+                raise RuntimeError(f"request {r} failed with status {info.status}")
+            batched += info.batch > 1
+        st = srv.stats()
+    return {
+        "requests": args.requests, "rate_per_s": args.rate, "size_law": "floor(2^U(10,27))",
+        "elements": int(sizes.sum()), "slots": args.serve_slots, "digit_bits": 16,
+        "latency_p50_ms": round(st.latency_p50_ms, 3), "latency_p99_ms": round(st.latency_p99_ms, 3),
+        "service_p50_ms": round(st.service_p50_ms, 3), "service_p99_ms": round(st.service_p99_ms, 3),
+        "value": round(st.elements_per_s / 1e6, 3), "unit": UNIT, "wall_ms": round(st.wall_ms, 1),
+        "batched_requests": int(st.batched_requests), "units": int(st.units),
+        "peak_hbm_gb": round(st.peak_bytes / 1e9, 3), "budget_hbm_gb": round(st.budget_bytes / 1e9, 3),
+        "offered_melem_s": round(float(sizes.mean()) * args.rate / 1e6, 1),
+    }
 
 
 def main(argv=None):
