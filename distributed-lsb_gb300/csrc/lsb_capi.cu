@@ -97,7 +97,19 @@ static bool wide_digits_split() {
   return !(e && std::strcmp(e, "task") == 0);
 }
 
-int plan_layout(int64_t n, int bits, int num_digits, Layout* L, bool allow_split) {
+// Look-back ring slots for `tiles` tiles of 2^bits status words: one slot per
+// tile while that costs at most an eighth of the array's bytes (or 64 MiB),
+// so that no slot is ever reused within a pass and tiles never wait for the
+// readers of a slot; otherwise (and for `compact` layouts) a ring a few grids
+// deep whose slots are reused once their readers are done.
+uint32_t ring_slots(uint64_t n, uint32_t tiles, int bits, uint32_t grid, bool compact) {
+  const uint64_t slot_bytes = (uint64_t)8u << bits;
+  const uint64_t cap = std::max<uint64_t>(64ull << 20, n * 2u);
+  if (!compact && (uint64_t)tiles * slot_bytes <= cap) return std::max<uint32_t>(1u, tiles);
+  return std::max<uint32_t>(1u, std::min<uint32_t>(tiles, 4u * grid + 64u));
+}
+
+int plan_layout(int64_t n, int bits, int num_digits, Layout* L, bool allow_split, bool compact) {
   DeviceInfo dev;
   if (int rc = current_device_info(&dev)) return rc;
   *L = Layout();
@@ -122,7 +134,7 @@ int plan_layout(int64_t n, int bits, int num_digits, Layout* L, bool allow_split
     L->tile_elems = onesweep_tile_elems(bits);
     L->grid = onesweep_grid(bits, dev, L->n);
     const uint32_t tiles = (uint32_t)((n + L->tile_elems - 1) / L->tile_elems);
-    L->ring_tiles = std::max<uint32_t>(1u, std::min<uint32_t>(tiles, 4u * L->grid + 64u));
+    L->ring_tiles = ring_slots((uint64_t)n, tiles, bits, L->grid, compact);
     L->off_hist = off;
     off = align_up(off + (size_t)num_digits * nbins * 4u, 256);
     L->off_gstart = off;

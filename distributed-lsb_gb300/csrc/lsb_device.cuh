@@ -18,10 +18,14 @@ constexpr int kMaxPasses = 64;  // digit_bits = 1 gives 64 passes
 // Device status codes (same values as include/lsb.h).
 constexpr uint32_t kStatusOk = 0;
 constexpr uint32_t kStatusTimeout = 6;
+// a run of equal digits reaching past the end of the array: the keys changed
+// while they were being sorted (LSB_ERR_INVALID_ARG)
+constexpr uint32_t kStatusInconsistent = 1;
 
 // Where a bounded wait ran out (ctrl->err_where), for diagnostics.
 constexpr uint32_t kWhereLookback = 1;
 constexpr uint32_t kWhereRingReuse = 2;
+constexpr uint32_t kWhereScatter = 3;
 
 // Spin limit for every device-side wait: after this many polls (with a
 // nanosleep back-off of up to 256 ns each) the kernel records
@@ -59,6 +63,12 @@ struct SegDesc {
   int num_passes = 0;
 };
 
+// Bytes of the onesweep kernel's per-warp counters ([bins][wp] entries of
+// cnt_size bytes), rounded up to 16 so that they clear with 16-byte stores.
+__host__ __device__ constexpr size_t onesweep_counter_bytes(uint32_t nbins, int wp, size_t cnt_size) {
+  return ((size_t)nbins * (size_t)wp * cnt_size + 15u) / 16u * 16u;
+}
+
 struct __align__(16) Elem {
   uint64_t key;
   uint64_t val;
@@ -92,6 +102,11 @@ __device__ __forceinline__ uint64_t ld_relaxed_u64(const uint64_t* p) {
 }
 __device__ __forceinline__ void st_relaxed_u64(uint64_t* p, uint64_t v) {
   asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+__device__ __forceinline__ uint32_t ld_relaxed_u32(const uint32_t* p) {
+  uint32_t v;
+  asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
 }
 __device__ __forceinline__ uint32_t ld_acquire_u32(const uint32_t* p) {
   uint32_t v;
@@ -128,6 +143,13 @@ __device__ __forceinline__ void fence_mbar_init() {
 }
 // orders this thread's earlier generic-proxy shared-memory accesses before
 // later async-proxy (bulk copy) writes to the same memory
+// named CTA barriers (id 0 is __syncthreads): `count` threads, whole warps
+__device__ __forceinline__ void named_bar_sync(int id, int count) {
+  asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory");
+}
+__device__ __forceinline__ void named_bar_arrive(int id, int count) {
+  asm volatile("bar.arrive %0, %1;" ::"r"(id), "r"(count) : "memory");
+}
 __device__ __forceinline__ void fence_proxy_async_smem() {
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 }
@@ -135,6 +157,20 @@ __device__ __forceinline__ void mbar_arrive_expect_tx(uint32_t bar, uint32_t byt
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
                : "memory");
 }
+// shared -> global bulk copy (async proxy) in the issuing thread's current bulk
+// group; src and dst 16-byte aligned, bytes a multiple of 16
+__device__ __forceinline__ void bulk_s2g(void* dst, uint32_t src, uint32_t bytes) {
+  asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(dst), "r"(src),
+               "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+// returns once the shared-memory sources of this thread's bulk copies have been read
+__device__ __forceinline__ void bulk_wait_read_all() {
+  asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+}
+// returns once this thread's bulk copies have completed
+__device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
 // global -> shared bulk copy; src and dst 16-byte aligned, bytes a multiple of 16
 __device__ __forceinline__ void bulk_g2s(uint32_t dst, const void* src, uint32_t bytes,
                                          uint32_t bar) {

@@ -56,7 +56,9 @@ struct Layout {
 
 // allow_split: digits of 12, 14 or 16 bits may run as two half-width
 // onesweep sub-passes each (sorts only; see lsb_capi.cu).
-int plan_layout(int64_t n, int bits, int num_digits, Layout* out, bool allow_split = false);
+int plan_layout(int64_t n, int bits, int num_digits, Layout* out, bool allow_split = false,
+                bool compact = false);
+uint32_t ring_slots(uint64_t n, uint32_t tiles, int bits, uint32_t grid, bool compact);
 
 // Runs passes [first_digit, first_digit + L.num_digits) over buffers X and Y.
 // Pass data starts in X. When target_parity is 0 the result ends in X (sort),

@@ -66,7 +66,7 @@ extern "C" int lsb_sort_pairs_noalloc(lsb_elem_t* d_a, lsb_elem_t* d_b, int64_t 
   void* ws = nullptr;
   if (int rc = noalloc_scratch(&ws)) return rc;
   Layout L;
-  if (int rc = plan_layout(n, digit_bits, lsb_num_passes(digit_bits), &L)) return rc;
+  if (int rc = plan_layout(n, digit_bits, lsb_num_passes(digit_bits), &L, false, true)) return rc;
   if (L.total > kNoallocScratchBytes) return LSB_ERR_WORKSPACE;
   cudaStream_t st = (cudaStream_t)stream;
   int rc = run_passes(reinterpret_cast<Elem*>(d_a), reinterpret_cast<Elem*>(d_b), 0, 0, ws, L, st);

@@ -202,12 +202,17 @@ __device__ __forceinline__ uint64_t wait_status(const uint64_t* p, uint32_t tag,
 }
 
 // Sums the look-back of digit `b` for tile t: walks predecessors t-1, t-2, ...
-// four status words at a time (independent loads), adding aggregates until an
+// WN status words at a time (independent loads), adding aggregates until an
 // inclusive prefix is found. Returns the number of digit-b elements in tiles
 // [0, t). Bounded: a predecessor that stays unpublished for kSpinLimit polls
 // (or an error raised elsewhere) ends the walk with *timed_out set.
+// The window sets the look-back's pace: one window costs one L2 round trip,
+// and all CTAs together must walk past about as many tiles as they finish in
+// that time, so a window much smaller than (CTAs x L2 latency / tile time)
+// makes the look-back, not the memory, bound the pass.
 constexpr int kLookbackWindow = 8;
 
+template <int WN>
 __device__ __forceinline__ uint32_t lookback_digit(const uint64_t* __restrict__ ring,
                                                    uint32_t ring_tiles, uint32_t nbins, uint32_t b,
                                                    int pass, uint32_t t, Ctrl* ctrl,
@@ -217,7 +222,6 @@ __device__ __forceinline__ uint32_t lookback_digit(const uint64_t* __restrict__ 
   int64_t j = (int64_t)t - 1;
   uint32_t polls = 0, ns = 8;
   while (j >= 0) {
-    constexpr int WN = kLookbackWindow;
     const int cnt = j >= WN - 1 ? WN : (int)j + 1;
     uint64_t s[WN];
 #pragma unroll
@@ -255,11 +259,26 @@ __device__ __forceinline__ uint32_t lookback_digit(const uint64_t* __restrict__ 
 }
 
 // One pass over the tiles of the input (persistent CTAs, tiles in input order).
-// CNT: per-warp digit counter type (uint16_t when 2^b x warps x 4 bytes would
-// not fit beside the staging buffer; a tile never exceeds 65535 elements).
-// Each CTA takes its next tile from the ticket and issues that tile's loads as
-// soon as the current tile is staged in shared memory, so the loads are in
-// flight during the current tile's look-back and stores.
+// CNT: per-warp digit counter type (uint16_t for wide digits, where 2^b x
+// (warps + 1) x 4 bytes would crowd shared memory; a tile never exceeds 65535
+// elements). Shared memory holds, side by side, the staging buffer (the tile
+// in digit order, E x 16 B), the per-warp counters [bin][W+1] and three
+// per-bin arrays (tile-local start, global start, count).
+// Per tile:
+//   1. digits of the tile, whose loads were issued during the previous tile;
+//   2. stable rank inside each warp (ballot peers, per-warp counters);
+//   3. per-bin row sums, published at once (so that later tiles can use
+//      them), scan of the bin totals, per-(bin, warp) starts written back;
+//   4. stage the tile in digit order;
+//   5. decoupled look-back per bin -> global start of each bin; issue the
+//      next tile's loads;
+//   6. the stores: up to 256 bins one bulk copy (shared -> global, async
+//      proxy) per run of equal digits, which drains while the next tile is
+//      ranked; above, 16-byte stores by every thread.
+// The next tile's ticket and the ring-slot reuse tags are fetched at the start
+// of a tile, so their latency overlaps the ranking. Up to 256 bins each warp
+// clears its own counter column after staging, so no barrier separates a
+// tile's stores from the next tile's ranking.
 // BITS > 0 fixes the digit width at compile time (8 and 11: the common widths);
 // BITS == 0 takes it from `bits_rt`.
 template <int THREADS, int K, int MINB, typename CNT, int BITS>
@@ -273,18 +292,21 @@ __global__ void __launch_bounds__(THREADS, MINB)
   static_assert(E <= 65535, "16-bit counters");
   constexpr uint32_t kSentinel = 0xffffffffu;
   extern __shared__ __align__(16) unsigned char smem[];
-  __shared__ uint32_t s_tile, s_next, s_err;
-  __shared__ uint32_t s_wt[33];
+  __shared__ uint32_t s_tile, s_next;
+  __shared__ uint32_t s_err[2];
+  __shared__ uint32_t s_wt[W];
 
   if (pass_skipped(ctrl, pass)) return;
   const int bits = BITS > 0 ? BITS : bits_rt;
   const uint32_t nbins = 1u << bits, mask = nbins - 1u;
   const int shift = bits * digit;  // `pass` indexes this call's passes, `digit` the key
-  const size_t stage_bytes = std::max<size_t>((size_t)E * sizeof(Elem), (size_t)nbins * WP * sizeof(CNT));
-  Elem* stage = reinterpret_cast<Elem*>(smem);   // tile in digit order
-  CNT* wcnt = reinterpret_cast<CNT*>(smem);      // per-warp counters [bin][WP], aliased
-  uint32_t* base = reinterpret_cast<uint32_t*>(smem + stage_bytes);  // [nbins]
-  uint32_t* tcount = base + nbins;                                    // [nbins]
+  const uint32_t cnt_words = (uint32_t)(onesweep_counter_bytes(nbins, WP, sizeof(CNT)) / 16u);
+  const bool column_clear = nbins <= 256u;
+  Elem* stage = reinterpret_cast<Elem*>(smem);                         // [E] tile in digit order
+  CNT* wcnt = reinterpret_cast<CNT*>(smem + (size_t)E * sizeof(Elem));  // [nbins][WP]
+  uint32_t* tstart = reinterpret_cast<uint32_t*>(smem + (size_t)E * sizeof(Elem) + (size_t)cnt_words * 16u);
+  uint32_t* gbase = tstart + nbins;   // [nbins] destination of the bin's first element
+  uint32_t* tcount = gbase + nbins;   // [nbins] this tile's count of each bin
 
   const uint32_t par = ctrl->parity[pass];
   const Elem* __restrict__ src = par ? Y : X;
@@ -293,6 +315,8 @@ __global__ void __launch_bounds__(THREADS, MINB)
   const uint32_t num_tiles = segmented ? *seg.num_tiles : (n + E - 1) / E;
   const uint32_t warp = threadIdx.x >> 5, lane = lane_id();
   const uint32_t lt = lanemask_lt();
+  // bins per thread in the scan: thread i owns bins [i*bpt, i*bpt + bpt)
+  const uint32_t bpt = (nbins + THREADS - 1) / THREADS;
 
   // where tile t lives: one array, or tile j of segment s of a batch (the
   // first tile of every segment starts its own look-back chain)
@@ -323,48 +347,64 @@ __global__ void __launch_bounds__(THREADS, MINB)
   };
 
   Elem v[K];
-  uint32_t d[K];
   // loads tile `t` warp-striped: item k of lane l in warp w is tile element
-  // w*32*K + k*32 + l (coalesced 512-byte warp loads)
+  // w*32*K + k*32 + l (coalesced 512-byte warp loads). Only issues the loads:
+  // nothing here waits for the data.
   auto load_tile = [&](uint32_t t) {
     const TileInfo ti = tile_info(t);
-    const uint32_t tile_begin = ti.begin;
-    const uint32_t len = ti.len;
-    const Elem* p = src + tile_begin + warp * 32u * K + lane;
-    if (len == E) {
+    const Elem* p = src + ti.begin + warp * 32u * K + lane;
+    if (ti.len == E) {
 #pragma unroll
       for (int k = 0; k < K; k++) v[k] = load_elem_stream(p + k * 32);
-#pragma unroll
-      for (int k = 0; k < K; k++) d[k] = digit_of(v[k].key, shift, mask);
     } else {
 #pragma unroll
-      for (int k = 0; k < K; k++) {
-        const uint32_t s = warp * 32u * K + (uint32_t)k * 32u + lane;
-        if (s < len) {
-          v[k] = load_elem_stream(p + k * 32);
-          d[k] = digit_of(v[k].key, shift, mask);
-        } else {
-          d[k] = kSentinel;
-        }
-      }
+      for (int k = 0; k < K; k++)
+        if (warp * 32u * K + (uint32_t)k * 32u + lane < ti.len) v[k] = load_elem_stream(p + k * 32);
     }
   };
+  auto clear_counters = [&]() {
+    uint4* z = reinterpret_cast<uint4*>(wcnt);
+    for (uint32_t i = threadIdx.x; i < cnt_words; i += THREADS) z[i] = make_uint4(0, 0, 0, 0);
+  };
 
+  clear_counters();
   if (threadIdx.x == 0) s_tile = atomicAdd(&ctrl->ticket[pass], 1u);
   __syncthreads();
   uint32_t t = s_tile;
   if (t < num_tiles) load_tile(t);
-  uint32_t lb_steps = 0, lb_polls = 0;
+  uint32_t lb_steps = 0, lb_polls = 0, iter = 0;
 
   while (t < num_tiles) {
     const TileInfo ti = tile_info(t);
     const uint32_t tile_len = ti.len;
-    if (threadIdx.x == 0) s_err = 0u;
-    for (uint32_t i = threadIdx.x; i < nbins * WP; i += THREADS) wcnt[i] = 0;
-    __syncthreads();
-
-    // 1. stable rank inside each warp: peers with the same digit, in item order
     const bool full = tile_len == E;  // every item valid: no sentinel tests
+    const uint32_t slot = t % ring_tiles;
+    const uint32_t tag = ring_tag(pass, t);
+    uint32_t* err = &s_err[iter & 1u];
+
+    // global accesses whose results are needed only after the ranking
+    uint32_t ticket = 0;
+    if (threadIdx.x == 0) {
+      ticket = atomicAdd(&ctrl->ticket[pass], 1u);
+      *err = 0u;
+    }
+    // ring slot reuse: the slot still holds tile x = t - ring_tiles, whose
+    // readers are the tiles (x, x + gridDim.x] (a tile looks back at most past
+    // the tiles in flight when it was dispatched); fetch their done tags now
+    const bool reuse = t >= ring_tiles;
+    const uint32_t x = t - ring_tiles;
+    uint32_t done_tag = 0;
+    const bool checker = reuse && threadIdx.x < gridDim.x && x + 1u + threadIdx.x < t;
+    if (checker) done_tag = ld_relaxed_u32(done + (x + 1u + threadIdx.x) % ring_tiles);
+
+    // 1. digits
+    uint32_t d[K];
+#pragma unroll
+    for (int k = 0; k < K; k++)
+      d[k] = (full || warp * 32u * K + (uint32_t)k * 32u + lane < tile_len)
+                 ? digit_of(v[k].key, shift, mask) : kSentinel;
+
+    // 2. stable rank inside each warp: peers with the same digit, in item order
     uint32_t r[K];
     if (full) {
 #pragma unroll
@@ -391,24 +431,18 @@ __global__ void __launch_bounds__(THREADS, MINB)
         __syncwarp();
       }
     }
-    __syncthreads();
-
-    // 2. the tile's count of every digit, published at once so that later
-    //    tiles can use it while this one is still working
-    const uint32_t slot = t % ring_tiles;
-    const uint32_t tag = ring_tag(pass, t);
     bool timed_out = false;
-    if (t >= ring_tiles) {
-      // the slot still holds tile t - ring_tiles; its readers are the tiles
-      // (x, x + gridDim.x] (each looks back at most past the tiles that were
-      // in flight when it was dispatched), so wait until they are done.
-      const uint32_t x = t - ring_tiles;
-      for (uint32_t j = 1 + threadIdx.x; j <= gridDim.x; j += THREADS) {
+    if (reuse) {
+      // every reader of the old slot must be done before this tile publishes;
+      // the tags read above usually already say so. Threads past the first
+      // THREADS readers (grids larger than a CTA) poll theirs here.
+      for (uint32_t j = 1u + threadIdx.x; j <= gridDim.x; j += THREADS) {
         const uint32_t y = x + j;
         if (y >= t) break;
         const uint32_t want = ring_tag(pass, y);
+        uint32_t got = (j == 1u + threadIdx.x) ? done_tag : ld_relaxed_u32(done + y % ring_tiles);
         uint32_t ns = 8, it = 0;
-        while (ld_acquire_u32(done + (y % ring_tiles)) < want) {
+        while (got < want) {
           if (++it >= kSpinLimit || ((it & 63u) == 0u && error_raised(ctrl))) {
             record_error(ctrl, kStatusTimeout, kWhereRingReuse);
             timed_out = true;
@@ -416,92 +450,136 @@ __global__ void __launch_bounds__(THREADS, MINB)
           }
           __nanosleep(ns);
           if (ns < 256) ns <<= 1;
+          got = ld_relaxed_u32(done + y % ring_tiles);
         }
         if (timed_out) break;
       }
-      __syncthreads();  // every reader of the old tile is done before any thread overwrites it
+      // acquire: the readers' done releases happen before this tile's writes
+      // to the slot (the fence follows the relaxed reads that observed them)
+      if (checker) __threadfence();
     }
-    uint64_t* my = ring + (size_t)slot * nbins;
-    for (uint32_t b = threadIdx.x; b < nbins; b += THREADS) {
-      uint32_t c = 0;
-#pragma unroll
-      for (int w = 0; w < W; w++) c += wcnt[b * WP + w];
-      tcount[b] = c;
-      st_relaxed_u64(my + b, pack_status(ti.first ? kFlagIncl : kFlagAgg, tag, c));
-    }
+    if (threadIdx.x == 0) s_next = ticket;
+    // the staging buffer is about to be overwritten: the previous tile's bulk
+    // copies (issued by this thread, if any) must have read it
+    bulk_wait_read_all();
+    __syncthreads();
 
-    // 3. exclusive scan of the counters in [digit][warp] order: the start of
-    //    each (digit, warp) group in the digit-sorted tile
+    uint64_t* my = ring + (size_t)slot * nbins;
+    const uint32_t t_next = s_next;
+    // 3. per-bin totals of the tile (published at once), scan of the totals,
+    //    per-(bin, warp) starts in the digit-sorted tile written back into
+    //    the counters, the tile-local start of each bin into tstart[]
     {
-      const uint32_t entries = nbins * W;
-      const uint32_t per = (entries + THREADS - 1) / THREADS;
-      const uint32_t lo = min(threadIdx.x * per, entries), hi = min(lo + per, entries);
+      const uint32_t b0 = threadIdx.x * bpt, b1 = min(b0 + bpt, nbins);
       uint32_t sum = 0;
-      // logical entry i = (bin i / W, warp i % W) lives at (i / W) * WP + i % W
-      for (uint32_t i = lo; i < hi; i++) sum += wcnt[(i / W) * WP + i % W];
-      uint32_t tot;
-      uint32_t ex = block_exclusive_scan(sum, s_wt, &tot);
-      for (uint32_t i = lo; i < hi; i++) {
-        CNT* p = &wcnt[(i / W) * WP + i % W];
-        const uint32_t c = *p;
-        *p = (CNT)ex;
-        ex += c;
+      for (uint32_t b = b0; b < b1; b++) {
+        uint32_t c = 0;
+#pragma unroll
+        for (int w = 0; w < W; w++) c += wcnt[b * WP + w];
+        tcount[b] = c;
+        st_relaxed_u64(my + b, pack_status(ti.first ? kFlagIncl : kFlagAgg, tag, c));
+        sum += c;
+      }
+      // exclusive scan of `sum` over the CTA (bins are owned in thread order)
+      uint32_t inc = sum;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= (uint32_t)o) inc += y;
+      }
+      if (lane == 31) s_wt[warp] = inc;
+      __syncthreads();
+      uint32_t off = inc - sum;
+#pragma unroll
+      for (int w = 0; w < W; w++)
+        if ((uint32_t)w < warp) off += s_wt[w];
+      for (uint32_t b = b0; b < b1; b++) {
+        tstart[b] = off;
+#pragma unroll
+        for (int w = 0; w < W; w++) {
+          CNT* p = &wcnt[b * WP + w];
+          const uint32_t c = *p;
+          *p = (CNT)off;
+          off += c;
+        }
       }
     }
     __syncthreads();
-    for (uint32_t b = threadIdx.x; b < nbins; b += THREADS) base[b] = wcnt[b * WP];
+    // 4. stage this thread's items in digit order (made visible to the bulk
+    //    copies); up to 256 bins each warp then clears its own counter column
 #pragma unroll
     for (int k = 0; k < K; k++)
-      if (full || d[k] != kSentinel) r[k] += wcnt[d[k] * WP + warp];
-    if (threadIdx.x == 0) s_next = atomicAdd(&ctrl->ticket[pass], 1u);
-    __syncthreads();
-
-    // 4. stage the tile in digit order (the counters are dead: stage aliases
-    //    them), then start loading the next tile into the freed registers
-#pragma unroll
-    for (int k = 0; k < K; k++)
-      if (full || d[k] != kSentinel) stage[r[k]] = v[k];
-    const uint32_t t_next = s_next;
-    if (t_next < num_tiles) load_tile(t_next);
-
-    // 5. decoupled look-back per digit
+      if (full || d[k] != kSentinel) stage[r[k] + wcnt[d[k] * WP + warp]] = v[k];
+    fence_proxy_async_smem();
+    if (column_clear) {
+      __syncwarp();
+      for (uint32_t b = lane; b < nbins; b += 32u) wcnt[b * WP + warp] = 0;
+    }
+    // 5. decoupled look-back per bin
     for (uint32_t b = threadIdx.x; b < nbins; b += THREADS) {
       uint32_t excl = 0;
       if (!ti.first) {
-        excl = lookback_digit(ring, ring_tiles, nbins, b, pass, t, ctrl, &timed_out, &lb_steps,
-                              &lb_polls);
+        excl = lookback_digit<kLookbackWindow>(ring, ring_tiles, nbins, b, pass, t, ctrl,
+                                               &timed_out, &lb_steps, &lb_polls);
         st_relaxed_u64(my + b, pack_status(kFlagIncl, tag, excl + tcount[b]));
       }
-      base[b] = ti.seg_base + ti.gs[b] + excl - base[b];  // dst = base[digit] + sorted position
+      gbase[b] = ti.seg_base + ti.gs[b] + excl;
     }
-    if (timed_out) s_err = 1u;
+    // the next tile's loads, into the registers freed by the staging (issued
+    // after the look-back: loads in flight slow the look-back's own loads)
+    if (t_next < num_tiles) load_tile(t_next);
+    if (timed_out) *err = 1u;
     __syncthreads();
     if (threadIdx.x == 0) {
       __threadfence();
       st_release_u32(done + slot, tag);  // look-back of tile t finished
     }
 
-    // 6. write runs of equal digits with coalesced 16-byte stores
-    if (!s_err) {
+    // 6. the stores: up to 256 bins one bulk copy per run of equal digits
+    //    (issued after the look-back: copies in flight slow the look-back's
+    //    loads), above that coalesced 16-byte stores of the staged tile
+    if (!*err && column_clear) {
+      bool issued = false;
+      for (uint32_t b = threadIdx.x; b < nbins; b += THREADS) {
+        const uint32_t c = tcount[b];
+        if (c == 0) continue;
+        const uint32_t g = gbase[b];
+        if ((uint64_t)g + c > n) {
+          record_error(ctrl, kStatusInconsistent, kWhereScatter);
+          continue;
+        }
+        bulk_s2g(dst + g, smem_u32(stage + tstart[b]), c * (uint32_t)sizeof(Elem));
+        issued = true;
+      }
+      if (issued) bulk_commit();
+    }
+    if (!*err && !column_clear) {
       if (full) {
 #pragma unroll 4
         for (int k = 0; k < K; k++) {
           const uint32_t pos = threadIdx.x + (uint32_t)k * THREADS;
           const Elem e = stage[pos];
-          const uint32_t o = base[digit_of(e.key, shift, mask)] + pos;
+          const uint32_t dg = digit_of(e.key, shift, mask);
+          const uint32_t o = gbase[dg] - tstart[dg] + pos;
           if (o < n) store_elem(dst + o, e);
         }
       } else {
         for (uint32_t pos = threadIdx.x; pos < tile_len; pos += THREADS) {
           const Elem e = stage[pos];
-          const uint32_t o = base[digit_of(e.key, shift, mask)] + pos;
+          const uint32_t dg = digit_of(e.key, shift, mask);
+          const uint32_t o = gbase[dg] - tstart[dg] + pos;
           if (o < n) store_elem(dst + o, e);
         }
       }
     }
-    __syncthreads();
+    if (!column_clear) {
+      clear_counters();
+      __syncthreads();
+    }
     t = t_next;
+    iter++;
   }
+  bulk_wait_all();
   if (lb_steps) atomicAdd(&ctrl->lookback_steps, lb_steps);
   if (lb_polls) atomicAdd(&ctrl->lookback_polls, lb_polls);
 }
@@ -684,7 +762,7 @@ __global__ void __launch_bounds__(THREADS, 1)
     for (uint32_t b = threadIdx.x; b < nbins; b += THREADS) {
       uint32_t excl = 0;
       if (t > 0) {
-        excl = lookback_digit(ring, ring_tiles, nbins, b, pass, t, ctrl, &timed_out, &lb_steps,
+        excl = lookback_digit<kLookbackWindow>(ring, ring_tiles, nbins, b, pass, t, ctrl, &timed_out, &lb_steps,
                               &lb_polls);
         st_relaxed_u64(my + b, pack_status(kFlagIncl, tag, excl + tcount[b]));
       }
@@ -752,10 +830,13 @@ static int onesweep_variant() {
   return (v >= 0 && v <= 3) ? v : 0;
 }
 
+// staging buffer + per-warp counters + tstart[], gbase[] and tcount[]
 static size_t reg_kernel_smem(int bits, int threads, int k) {
-  const size_t nbins = (size_t)1 << bits, E = (size_t)threads * k;
+  const uint32_t nbins = 1u << bits;
+  const size_t E = (size_t)threads * k;
   const size_t cnt_bytes = bits <= 8 ? 4u : 2u;
-  return std::max(E * sizeof(Elem), nbins * (threads / 32 + 1) * cnt_bytes) + 2u * nbins * 4u;
+  return E * sizeof(Elem) + onesweep_counter_bytes(nbins, threads / 32 + 1, cnt_bytes) +
+         3u * (size_t)nbins * 4u;
 }
 static size_t tma_kernel_smem(int threads, int k) {
   const size_t E = (size_t)threads * k;

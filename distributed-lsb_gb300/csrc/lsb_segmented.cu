@@ -177,7 +177,7 @@ static int seg_plan_layout(int64_t n, int64_t nseg, int digit_bits, int variant,
   L->tile = onesweep_tile_elems_v(bits, variant);
   L->max_tiles = (uint32_t)(((uint64_t)n + L->tile - 1) / L->tile + (uint64_t)nseg);
   L->grid = onesweep_grid_v(bits, variant, dev, std::max<uint32_t>(1u, L->max_tiles));
-  L->ring_tiles = std::max<uint32_t>(1u, std::min<uint32_t>(L->max_tiles, 4u * L->grid + 64u));
+  L->ring_tiles = ring_slots((uint64_t)n, L->max_tiles, bits, L->grid, false);
   const size_t nbins = (size_t)1 << bits;
   size_t off = kCtrlBytes;
   L->off_tile0 = off;
