@@ -14,6 +14,7 @@
 namespace lsb {
 
 constexpr int kMaxPasses = 64;  // digit_bits = 1 gives 64 passes
+constexpr int kMaxOnesweepBits = 11;  // widest digit of the onesweep kernels
 
 // Device status codes (same values as include/lsb.h).
 constexpr uint32_t kStatusOk = 0;
@@ -143,13 +144,6 @@ __device__ __forceinline__ void fence_mbar_init() {
 }
 // orders this thread's earlier generic-proxy shared-memory accesses before
 // later async-proxy (bulk copy) writes to the same memory
-// named CTA barriers (id 0 is __syncthreads): `count` threads, whole warps
-__device__ __forceinline__ void named_bar_sync(int id, int count) {
-  asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory");
-}
-__device__ __forceinline__ void named_bar_arrive(int id, int count) {
-  asm volatile("bar.arrive %0, %1;" ::"r"(id), "r"(count) : "memory");
-}
 __device__ __forceinline__ void fence_proxy_async_smem() {
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 }

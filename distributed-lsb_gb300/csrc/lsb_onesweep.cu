@@ -206,11 +206,12 @@ __device__ __forceinline__ uint64_t wait_status(const uint64_t* p, uint32_t tag,
 // inclusive prefix is found. Returns the number of digit-b elements in tiles
 // [0, t). Bounded: a predecessor that stays unpublished for kSpinLimit polls
 // (or an error raised elsewhere) ends the walk with *timed_out set.
-// The window sets the look-back's pace: one window costs one L2 round trip,
-// and all CTAs together must walk past about as many tiles as they finish in
-// that time, so a window much smaller than (CTAs x L2 latency / tile time)
-// makes the look-back, not the memory, bound the pass.
+// Used where a thread has several bins (wide digits), whose walks run one
+// after another: there a window of 8 measured faster than one word per round.
 constexpr int kLookbackWindow = 8;
+// wide digits: walk a thread's bins interleaved, one word per bin per round
+// (true), or one bin after another with the window above (false)
+constexpr bool kWideInterleaved = true;
 
 template <int WN>
 __device__ __forceinline__ uint32_t lookback_digit(const uint64_t* __restrict__ ring,
@@ -256,6 +257,81 @@ __device__ __forceinline__ uint32_t lookback_digit(const uint64_t* __restrict__ 
   }
   *polls_out += polls;
   return excl;
+}
+
+// Decoupled look-back for the NB bins b0, b0 + stride, ... (< nbins) of this
+// thread: walks each bin's predecessors t-1, t-2, ... one status word per bin
+// per round, adding aggregates until it meets an inclusive prefix; the NB
+// bins' loads of a round are independent and in flight together. Writes the
+// number of elements of each bin in tiles [0, t) to excl[] and publishes each
+// bin's inclusive prefix (excl + count[b]) to `mine` with `tag` (with several
+// bins, as soon as that bin's walk ends, so later tiles' walks can stop
+// there; with one, after the walk). One status word
+// per round is deliberate: the walk usually ends one or two tiles back, and
+// on a GPU streaming at full bandwidth every extra L2 request (a wider window
+// read ahead) costs more than the extra round trips it might save.
+// Bounded: a predecessor that stays unpublished for kSpinLimit polls (or an
+// error raised elsewhere) ends the walk with *timed_out set.
+template <int NB>
+__device__ __forceinline__ void lookback_bins(const uint64_t* __restrict__ ring, uint32_t ring_tiles,
+                                              uint32_t nbins, uint32_t b0, uint32_t stride,
+                                              int pass, uint32_t t, uint32_t* excl,
+                                              uint64_t* mine, uint32_t tag,
+                                              const uint32_t* count, Ctrl* ctrl, bool* timed_out,
+                                              uint32_t* steps, uint32_t* polls_out) {
+  int64_t j[NB];
+  bool live[NB];
+  bool any = false;
+#pragma unroll
+  for (int i = 0; i < NB; i++) {
+    excl[i] = 0;
+    j[i] = (int64_t)t - 1;
+    live[i] = b0 + (uint32_t)i * stride < nbins && t > 0;
+    any |= live[i];
+  }
+  uint32_t polls = 0, ns = 8;
+  while (any) {
+    uint64_t s[NB];
+#pragma unroll
+    for (int i = 0; i < NB; i++)
+      if (live[i])
+        s[i] = ld_relaxed_u64(ring + (size_t)((uint32_t)j[i] % ring_tiles) * nbins + b0 +
+                              (uint32_t)i * stride);
+    *steps += 1;
+    bool moved = false;
+    any = false;
+#pragma unroll
+    for (int i = 0; i < NB; i++) {
+      if (live[i]) {
+        const uint64_t e = s[i];
+        if (status_tag(e) == ring_tag(pass, (uint32_t)j[i]) && status_flag(e) != 0) {
+          excl[i] += (uint32_t)e;
+          j[i]--;
+          moved = true;
+          if (status_flag(e) == kFlagIncl || j[i] < 0) {
+            live[i] = false;
+            const uint32_t b = b0 + (uint32_t)i * stride;
+            if (NB > 1) st_relaxed_u64(mine + b, pack_status(kFlagIncl, tag, excl[i] + count[b]));
+          }
+        }
+        any |= live[i];
+      }
+    }
+    if (any && !moved) {  // the nearest unconsumed predecessors have not published yet
+      if (++polls >= kSpinLimit || ((polls & 63u) == 0u && error_raised(ctrl))) {
+        record_error(ctrl, kStatusTimeout, kWhereLookback);
+        *timed_out = true;
+        break;
+      }
+      __nanosleep(ns);
+      if (ns < 256) ns <<= 1;
+    } else {
+      ns = 8;
+    }
+  }
+  if (NB == 1 && b0 < nbins && t > 0)
+    st_relaxed_u64(mine + b0, pack_status(kFlagIncl, tag, excl[0] + count[b0]));
+  *polls_out += polls;
 }
 
 // One pass over the tiles of the input (persistent CTAs, tiles in input order).
@@ -515,15 +591,35 @@ __global__ void __launch_bounds__(THREADS, MINB)
       __syncwarp();
       for (uint32_t b = lane; b < nbins; b += 32u) wcnt[b * WP + warp] = 0;
     }
-    // 5. decoupled look-back per bin
-    for (uint32_t b = threadIdx.x; b < nbins; b += THREADS) {
-      uint32_t excl = 0;
-      if (!ti.first) {
-        excl = lookback_digit<kLookbackWindow>(ring, ring_tiles, nbins, b, pass, t, ctrl,
-                                               &timed_out, &lb_steps, &lb_polls);
-        st_relaxed_u64(my + b, pack_status(kFlagIncl, tag, excl + tcount[b]));
+    // 5. decoupled look-back of this thread's bins b = threadIdx.x + i x THREADS
+    {
+      constexpr int NB = (BITS > 0 ? (1 << BITS) : (1 << kMaxOnesweepBits)) / THREADS > 0
+                             ? (BITS > 0 ? (1 << BITS) : (1 << kMaxOnesweepBits)) / THREADS
+                             : 1;
+      uint32_t excl[NB];
+#pragma unroll
+      for (int i = 0; i < NB; i++) excl[i] = 0;
+      if (!ti.first && (nbins <= (uint32_t)THREADS || kWideInterleaved)) {
+        lookback_bins<NB>(ring, ring_tiles, nbins, threadIdx.x, THREADS, pass, t, excl, my, tag,
+                          tcount, ctrl, &timed_out, &lb_steps, &lb_polls);
+      } else if (!ti.first) {
+        // several bins per thread: each bin's inclusive prefix is published
+        // as soon as its walk ends (later tiles' walks stop there)
+#pragma unroll
+        for (int i = 0; i < NB; i++) {
+          const uint32_t b = threadIdx.x + (uint32_t)i * THREADS;
+          if (b < nbins) {
+            excl[i] = lookback_digit<kLookbackWindow>(ring, ring_tiles, nbins, b, pass, t, ctrl,
+                                                      &timed_out, &lb_steps, &lb_polls);
+            st_relaxed_u64(my + b, pack_status(kFlagIncl, tag, excl[i] + tcount[b]));
+          }
+        }
       }
-      gbase[b] = ti.seg_base + ti.gs[b] + excl;
+#pragma unroll
+      for (int i = 0; i < NB; i++) {
+        const uint32_t b = threadIdx.x + (uint32_t)i * THREADS;
+        if (b < nbins) gbase[b] = ti.seg_base + ti.gs[b] + excl[i];
+      }
     }
     // the next tile's loads, into the registers freed by the staging (issued
     // after the look-back: loads in flight slow the look-back's own loads)
@@ -758,13 +854,13 @@ __global__ void __launch_bounds__(THREADS, 1)
       if (full || d[k] != kSentinel) stage[r[k] + wcnt[d[k] * WP + warp]] = v[k];
     __syncthreads();  // tile starts in base[] are read by the look-back threads
 
-    // 6. decoupled look-back per digit
-    for (uint32_t b = threadIdx.x; b < nbins; b += THREADS) {
+    // 6. decoupled look-back per digit (THREADS >= 256 >= nbins: one bin per thread)
+    if (threadIdx.x < nbins) {
+      const uint32_t b = threadIdx.x;
       uint32_t excl = 0;
       if (t > 0) {
-        excl = lookback_digit<kLookbackWindow>(ring, ring_tiles, nbins, b, pass, t, ctrl, &timed_out, &lb_steps,
-                              &lb_polls);
-        st_relaxed_u64(my + b, pack_status(kFlagIncl, tag, excl + tcount[b]));
+        lookback_bins<1>(ring, ring_tiles, nbins, b, THREADS, pass, t, &excl, my, tag, tcount,
+                         ctrl, &timed_out, &lb_steps, &lb_polls);
       }
       base[b] = gstart[b] + excl - base[b];  // dst = base[digit] + sorted position
     }
