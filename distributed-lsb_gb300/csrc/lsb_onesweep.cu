@@ -906,8 +906,9 @@ __global__ void __launch_bounds__(THREADS, 1)
 // Default (0): the register kernel, 512 threads x 16 items (8192-element
 // tiles, one CTA per SM), 32-bit counters up to 256 digits, 16-bit above.
 // LSB_ONESWEEP_VARIANT selects another shape (a tuning knob; measured on
-// GB300 at 2^30 elements, 8-bit digits, per pass: 0 -> 12.1 ms, 2 -> 15.5 ms,
-// 1 -> 15.8 ms, 3 -> 18.4 ms):
+// GB300 at 2^30 elements, 16-bit digits as eight 8-bit passes, per sort:
+// 0 -> 76.9 ms, 2 -> 87.0 ms, 1 -> 102.9 ms; 3 was the slowest when last
+// measured):
 //  1: bulk-copy kernel 768 x 8 (6144-element tiles, 24 warps) up to 256 digits;
 //  2: register kernel 256 x 16, two CTAs per SM;
 //  3: bulk-copy kernel 1024 x 4 (4096-element tiles, 32 warps) up to 256 digits.
