@@ -626,9 +626,12 @@ __global__ void __launch_bounds__(THREADS, MINB)
     if (t_next < num_tiles) load_tile(t_next);
     if (timed_out) *err = 1u;
     __syncthreads();
-    if (threadIdx.x == 0) {
+    // look-back of tile t finished: only a ring whose slots are reused needs
+    // to know (with one slot per tile nobody waits, and the fence would stall
+    // this thread behind its just-issued loads)
+    if (threadIdx.x == 0 && ring_tiles < num_tiles) {
       __threadfence();
-      st_release_u32(done + slot, tag);  // look-back of tile t finished
+      st_release_u32(done + slot, tag);
     }
 
     // 6. the stores: up to 256 bins one bulk copy per run of equal digits
@@ -866,7 +869,7 @@ __global__ void __launch_bounds__(THREADS, 1)
     }
     if (timed_out) s_err = 1u;
     __syncthreads();
-    if (threadIdx.x == 0) {
+    if (threadIdx.x == 0 && ring_tiles < num_tiles) {
       __threadfence();
       st_release_u32(done + slot, tag);
     }
