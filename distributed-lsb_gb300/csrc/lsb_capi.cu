@@ -578,6 +578,24 @@ int lsb_profile_enable(int on) {
   return LSB_OK;
 }
 
+int lsb_selftest_wait_timeout(void* stream, int* device_status) {
+  if (!device_status) return LSB_ERR_INVALID_ARG;
+  cudaStream_t st = (cudaStream_t)stream;
+  const size_t bytes = kCtrlBytes + 32u;
+  void* ws = nullptr;
+  if (int rc = pool_alloc(&ws, bytes, st)) return rc;
+  int rc = LSB_OK;
+  Ctrl c{};
+  if (cudaMemsetAsync(ws, 0, bytes, st) != cudaSuccess ||
+      lsb::selftest_lookback_timeout(static_cast<unsigned char*>(ws), st) != 0 ||
+      cudaMemcpyAsync(&c, ws, sizeof c, cudaMemcpyDeviceToHost, st) != cudaSuccess)
+    rc = LSB_ERR_CUDA;
+  cudaFreeAsync(ws, st);
+  if (cudaStreamSynchronize(st) != cudaSuccess && rc == LSB_OK) rc = LSB_ERR_CUDA;
+  if (rc == LSB_OK) *device_status = (int)c.error;
+  return rc;
+}
+
 int lsb_profile_read(lsb_kernel_time_t* out, int capacity, int* count) {
   if (!count || capacity < 0 || (capacity > 0 && !out)) return LSB_ERR_INVALID_ARG;
   std::vector<ProfRec> recs;

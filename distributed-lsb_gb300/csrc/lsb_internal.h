@@ -72,6 +72,9 @@ int onesweep_run(Elem* X, Elem* Y, int first_digit, int target_parity, unsigned 
 int task_run(Elem* X, Elem* Y, int first_digit, int target_parity, unsigned char* ws,
              const Layout& L, cudaStream_t st);
 uint32_t onesweep_tile_elems(int bits);
+// the look-back wait of the sort kernels on a predecessor that never publishes
+// (failure-detection self-test); ws: kCtrlBytes + 32 bytes, zeroed by the caller
+int selftest_lookback_timeout(unsigned char* ws, cudaStream_t st);
 // explicit kernel shape (variant 0: 512 threads x 16, 1 CTA/SM; 2: 256 x 16, 2 CTAs/SM)
 uint32_t onesweep_tile_elems_v(int bits, int variant);
 uint32_t onesweep_grid_v(int bits, int variant, const DeviceInfo& dev, uint32_t tiles);

@@ -1003,6 +1003,30 @@ uint32_t onesweep_grid(int bits, const DeviceInfo& dev, uint32_t n) {
 }
 
 // ---------------------------------------------------------------------------
+// failure-detection self-test: tile 1 of a one-bin pass waits for tile 0's
+// status word, which nothing publishes; the bounded wait must run out, record
+// kStatusTimeout in the control block and return
+
+__global__ void k_selftest_lookback(Ctrl* ctrl, uint64_t* ring) {
+  if (threadIdx.x != 0) return;
+  const uint32_t count = 0;
+  uint32_t excl = 0, steps = 0, polls = 0;
+  bool timed_out = false;
+  // ring: two one-bin slots; slot 0 (tile 0) stays zero, slot 1 receives
+  // tile 1's (meaningless) inclusive prefix after the timeout
+  lookback_bins<1>(ring, 2u, 1u, 0u, 1u, 0, 1u, &excl, ring + 1, ring_tag(0, 1u), &count, ctrl,
+                   &timed_out, &steps, &polls);
+  ctrl->lookback_polls = polls;
+}
+
+int selftest_lookback_timeout(unsigned char* ws, cudaStream_t st) {
+  Ctrl* ctrl = reinterpret_cast<Ctrl*>(ws);
+  uint64_t* ring = reinterpret_cast<uint64_t*>(ws + kCtrlBytes);
+  k_selftest_lookback<<<1, 32, 0, st>>>(ctrl, ring);
+  return cudaPeekAtLastError() == cudaSuccess ? 0 : 5;
+}
+
+// ---------------------------------------------------------------------------
 // copy back when an odd number of passes left the data in the other buffer
 
 __global__ void k_final_copy(Elem* X, Elem* Y, uint32_t n, int num_digits, int target_parity,

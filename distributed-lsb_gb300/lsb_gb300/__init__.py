@@ -67,6 +67,7 @@ SIGNATURES = {
     "lsb_server_destroy": (ctypes.c_int, [_P]),
     "lsb_profile_enable": (ctypes.c_int, [ctypes.c_int]),
     "lsb_profile_read": (ctypes.c_int, [_P, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]),
+    "lsb_selftest_wait_timeout": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int)]),
 }
 
 
@@ -372,6 +373,16 @@ def profile_read() -> dict:
     cnt = ctypes.c_int(0)
     _check(load().lsb_profile_read(ctypes.cast(arr, ctypes.c_void_p), 64, ctypes.byref(cnt)), "lsb_profile_read")
     return {arr[i].name.decode(): (arr[i].launches, arr[i].total_ms) for i in range(cnt.value)}
+
+
+def selftest_wait_timeout(stream=None) -> int:
+    """Runs the sort kernels' look-back wait on a predecessor that never
+    publishes; returns the device status it ended with (LSB_ERR_DEVICE_TIMEOUT
+    when the bounded wait ran out as designed). Takes about a second."""
+    st = ctypes.c_int(-1)
+    _check(load().lsb_selftest_wait_timeout(_stream_ptr(stream), ctypes.byref(st)),
+           "lsb_selftest_wait_timeout")
+    return st.value
 
 
 def verify(inp, out, stream=None) -> int:

@@ -282,6 +282,15 @@ typedef struct lsb_kernel_time {
 int lsb_profile_enable(int on);
 int lsb_profile_read(lsb_kernel_time_t* out, int capacity, int* count);
 
+/* Failure-detection self-test (no counterpart in the reference, which aborts
+ * on errors, mpi/mpi_lsbsort.cpp:18-20): runs the sort kernels' look-back
+ * wait on a predecessor that never publishes, in a scratch workspace of its
+ * own. The bounded wait runs out (about a second), the kernel records the
+ * timeout and returns; *device_status receives the status the sort entry
+ * points would return for it (LSB_ERR_DEVICE_TIMEOUT) and the context stays
+ * usable. Blocking; allocates a few KiB. */
+int lsb_selftest_wait_timeout(void* stream, int* device_status);
+
 #ifdef __cplusplus
 }
 #endif
