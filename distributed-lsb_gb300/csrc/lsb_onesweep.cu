@@ -634,36 +634,29 @@ __global__ void __launch_bounds__(THREADS, MINB)
       st_release_u32(done + slot, tag);
     }
 
-    // 6. the stores: up to 256 bins one bulk copy per run of equal digits
-    //    (issued after the look-back: copies in flight slow the look-back's
-    //    loads), above that coalesced 16-byte stores of the staged tile
-    if (!*err && column_clear) {
-      bool issued = false;
-      for (uint32_t b = threadIdx.x; b < nbins; b += THREADS) {
+    // 6. the stores (issued after the look-back: copies in flight slow the
+    //    look-back's loads). Bins [0, nbulk) leave shared memory by one bulk
+    //    copy each (shared -> global, issued by thread b): all bins up to 256
+    //    of them. The positions of the bins above nbulk, [tstart[nbulk],
+    //    tile_len), are written with coalesced 16-byte stores by the threads
+    //    that issue no bulk copy: above 256 bins that is the whole tile.
+    if (!*err) {
+      const uint32_t nbulk = column_clear ? nbins : 0u;
+      if (column_clear && threadIdx.x < nbins) {
+        const uint32_t b = threadIdx.x;
         const uint32_t c = tcount[b];
-        if (c == 0) continue;
-        const uint32_t g = gbase[b];
-        if ((uint64_t)g + c > n) {
-          record_error(ctrl, kStatusInconsistent, kWhereScatter);
-          continue;
-        }
-        bulk_s2g(dst + g, smem_u32(stage + tstart[b]), c * (uint32_t)sizeof(Elem));
-        issued = true;
-      }
-      if (issued) bulk_commit();
-    }
-    if (!*err && !column_clear) {
-      if (full) {
-#pragma unroll 4
-        for (int k = 0; k < K; k++) {
-          const uint32_t pos = threadIdx.x + (uint32_t)k * THREADS;
-          const Elem e = stage[pos];
-          const uint32_t dg = digit_of(e.key, shift, mask);
-          const uint32_t o = gbase[dg] - tstart[dg] + pos;
-          if (o < n) store_elem(dst + o, e);
+        if (c != 0) {
+          const uint32_t g = gbase[b];
+          if ((uint64_t)g + c > n) {
+            record_error(ctrl, kStatusInconsistent, kWhereScatter);
+          } else {
+            bulk_s2g(dst + g, smem_u32(stage + tstart[b]), c * (uint32_t)sizeof(Elem));
+            bulk_commit();
+          }
         }
       } else {
-        for (uint32_t pos = threadIdx.x; pos < tile_len; pos += THREADS) {
+        const uint32_t from = nbulk < nbins ? tstart[nbulk] : tile_len;
+        for (uint32_t pos = from + (threadIdx.x - nbulk); pos < tile_len; pos += THREADS - nbulk) {
           const Elem e = stage[pos];
           const uint32_t dg = digit_of(e.key, shift, mask);
           const uint32_t o = gbase[dg] - tstart[dg] + pos;
