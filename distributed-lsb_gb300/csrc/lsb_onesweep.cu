@@ -259,17 +259,50 @@ __device__ __forceinline__ uint32_t lookback_digit(const uint64_t* __restrict__ 
   return excl;
 }
 
+// Decoupled look-back of bin b for tile t: walks predecessors t-1, t-2, ...
+// one status word per round, adding aggregates until it meets an inclusive
+// prefix; returns the number of bin-b elements in tiles [0, t). One status
+// word per round is deliberate: the walk usually ends a few tiles back, and on
+// a GPU streaming at full bandwidth every extra L2 request (a wider window
+// read ahead) costs more than the extra round trips it might save. Bounded: a
+// predecessor that stays unpublished for kSpinLimit polls (or an error raised
+// elsewhere) ends the walk with *timed_out set.
+__device__ __forceinline__ uint32_t walk_one(const uint64_t* __restrict__ ring, uint32_t ring_tiles,
+                                             uint32_t nbins, uint32_t b, int pass, uint32_t t,
+                                             Ctrl* ctrl, bool* timed_out, uint32_t* steps,
+                                             uint32_t* polls_out) {
+  uint32_t excl = 0, polls = 0, ns = 8;
+  uint32_t j = t - 1;
+  for (;;) {
+    const uint64_t e = ld_relaxed_u64(ring + (size_t)(j % ring_tiles) * nbins + b);
+    *steps += 1;
+    if (status_tag(e) == ring_tag(pass, j) && status_flag(e) != 0) {
+      excl += (uint32_t)e;
+      if (status_flag(e) == kFlagIncl || j == 0) break;
+      j--;
+      ns = 8;
+      continue;
+    }
+    if (++polls >= kSpinLimit || ((polls & 63u) == 0u && error_raised(ctrl))) {
+      record_error(ctrl, kStatusTimeout, kWhereLookback);
+      *timed_out = true;
+      break;
+    }
+    __nanosleep(ns);
+    if (ns < 256) ns <<= 1;
+  }
+  *polls_out += polls;
+  return excl;
+}
+
 // Decoupled look-back for the NB bins b0, b0 + stride, ... (< nbins) of this
 // thread: walks each bin's predecessors t-1, t-2, ... one status word per bin
 // per round, adding aggregates until it meets an inclusive prefix; the NB
 // bins' loads of a round are independent and in flight together. Writes the
 // number of elements of each bin in tiles [0, t) to excl[] and publishes each
-// bin's inclusive prefix (excl + count[b]) to `mine` with `tag` (with several
-// bins, as soon as that bin's walk ends, so later tiles' walks can stop
-// there; with one, after the walk). One status word
-// per round is deliberate: the walk usually ends one or two tiles back, and
-// on a GPU streaming at full bandwidth every extra L2 request (a wider window
-// read ahead) costs more than the extra round trips it might save.
+// bin's inclusive prefix (excl + count[b]) to `mine` with `tag` as soon as
+// that bin's walk ends, so later tiles' walks can stop there (wide digits:
+// several bins per thread; one bin per thread uses walk_one).
 // Bounded: a predecessor that stays unpublished for kSpinLimit polls (or an
 // error raised elsewhere) ends the walk with *timed_out set.
 template <int NB>
@@ -311,7 +344,7 @@ __device__ __forceinline__ void lookback_bins(const uint64_t* __restrict__ ring,
           if (status_flag(e) == kFlagIncl || j[i] < 0) {
             live[i] = false;
             const uint32_t b = b0 + (uint32_t)i * stride;
-            if (NB > 1) st_relaxed_u64(mine + b, pack_status(kFlagIncl, tag, excl[i] + count[b]));
+            st_relaxed_u64(mine + b, pack_status(kFlagIncl, tag, excl[i] + count[b]));
           }
         }
         any |= live[i];
@@ -329,8 +362,6 @@ __device__ __forceinline__ void lookback_bins(const uint64_t* __restrict__ ring,
       ns = 8;
     }
   }
-  if (NB == 1 && b0 < nbins && t > 0)
-    st_relaxed_u64(mine + b0, pack_status(kFlagIncl, tag, excl[0] + count[b0]));
   *polls_out += polls;
 }
 
@@ -599,7 +630,14 @@ __global__ void __launch_bounds__(THREADS, MINB)
       uint32_t excl[NB];
 #pragma unroll
       for (int i = 0; i < NB; i++) excl[i] = 0;
-      if (!ti.first && (nbins <= (uint32_t)THREADS || kWideInterleaved)) {
+      if (!ti.first && nbins <= (uint32_t)THREADS) {
+        if (threadIdx.x < nbins) {
+          excl[0] = walk_one(ring, ring_tiles, nbins, threadIdx.x, pass, t, ctrl, &timed_out,
+                             &lb_steps, &lb_polls);
+          st_relaxed_u64(my + threadIdx.x,
+                         pack_status(kFlagIncl, tag, excl[0] + tcount[threadIdx.x]));
+        }
+      } else if (!ti.first && kWideInterleaved) {
         lookback_bins<NB>(ring, ring_tiles, nbins, threadIdx.x, THREADS, pass, t, excl, my, tag,
                           tcount, ctrl, &timed_out, &lb_steps, &lb_polls);
       } else if (!ti.first) {
@@ -855,8 +893,8 @@ __global__ void __launch_bounds__(THREADS, 1)
       const uint32_t b = threadIdx.x;
       uint32_t excl = 0;
       if (t > 0) {
-        lookback_bins<1>(ring, ring_tiles, nbins, b, THREADS, pass, t, &excl, my, tag, tcount,
-                         ctrl, &timed_out, &lb_steps, &lb_polls);
+        excl = walk_one(ring, ring_tiles, nbins, b, pass, t, ctrl, &timed_out, &lb_steps, &lb_polls);
+        st_relaxed_u64(my + b, pack_status(kFlagIncl, tag, excl + tcount[b]));
       }
       base[b] = gstart[b] + excl - base[b];  // dst = base[digit] + sorted position
     }
@@ -1002,13 +1040,11 @@ uint32_t onesweep_grid(int bits, const DeviceInfo& dev, uint32_t n) {
 
 __global__ void k_selftest_lookback(Ctrl* ctrl, uint64_t* ring) {
   if (threadIdx.x != 0) return;
-  const uint32_t count = 0;
-  uint32_t excl = 0, steps = 0, polls = 0;
+  uint32_t steps = 0, polls = 0;
   bool timed_out = false;
-  // ring: two one-bin slots; slot 0 (tile 0) stays zero, slot 1 receives
-  // tile 1's (meaningless) inclusive prefix after the timeout
-  lookback_bins<1>(ring, 2u, 1u, 0u, 1u, 0, 1u, &excl, ring + 1, ring_tag(0, 1u), &count, ctrl,
-                   &timed_out, &steps, &polls);
+  // ring: two one-bin slots; slot 0 (tile 0) stays zero, so tile 1's walk
+  // never finds a published predecessor
+  (void)walk_one(ring, 2u, 1u, 0u, 0, 1u, ctrl, &timed_out, &steps, &polls);
   ctrl->lookback_polls = polls;
 }
 
