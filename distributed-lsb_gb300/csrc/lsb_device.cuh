@@ -197,15 +197,18 @@ __device__ __forceinline__ Elem lds_elem(const Elem* p) {
 }
 
 // Lanes of the warp whose `bits`-bit value v equals this lane's, from one
-// ballot per bit (ALU work instead of the match unit). `valid` lanes only
-// match valid lanes.
+// ballot per bit (ALU work instead of the match unit): a lane keeps the lanes
+// whose bit i equals its own, i.e. the ballot b where its bit is set and ~b
+// where it is clear, written b ^ (bit - 1) (one AND-XOR per bit; measured
+// faster than selecting between b and ~b). `valid` lanes only match valid
+// lanes.
 __device__ __forceinline__ uint32_t warp_peers(uint32_t v, int bits, bool valid) {
   const uint32_t vm = __ballot_sync(0xffffffffu, valid);
   uint32_t peers = valid ? vm : ~vm;
   for (int i = 0; i < bits; i++) {
-    const bool bit = (v >> i) & 1u;
+    const uint32_t bit = (v >> i) & 1u;
     const uint32_t b = __ballot_sync(0xffffffffu, bit);
-    peers &= bit ? b : ~b;
+    peers &= b ^ (bit - 1u);
   }
   return peers;
 }
@@ -214,9 +217,9 @@ __device__ __forceinline__ uint32_t warp_peers_fixed(uint32_t v) {
   uint32_t peers = 0xffffffffu;
 #pragma unroll
   for (int i = 0; i < BITS; i++) {
-    const bool bit = (v >> i) & 1u;
+    const uint32_t bit = (v >> i) & 1u;
     const uint32_t b = __ballot_sync(0xffffffffu, bit);
-    peers &= bit ? b : ~b;
+    peers &= b ^ (bit - 1u);
   }
   return peers;
 }
