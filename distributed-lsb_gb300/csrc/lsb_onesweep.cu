@@ -522,7 +522,7 @@ __global__ void __launch_bounds__(THREADS, MINB)
         const uint32_t c = *cp;
         r[k] = c + __popc(peers & lt);
         __syncwarp();
-        if (lane == (uint32_t)(__ffs(peers) - 1)) *cp = (CNT)(c + __popc(peers));
+        *cp = (CNT)(c + __popc(peers));  // every peer writes the same count: no leader test
         __syncwarp();
       }
     } else {
@@ -533,8 +533,7 @@ __global__ void __launch_bounds__(THREADS, MINB)
         if (d[k] != kSentinel) c = wcnt[d[k] * WP + warp];
         r[k] = c + __popc(peers & lt);
         __syncwarp();
-        if (d[k] != kSentinel && lane == (uint32_t)(__ffs(peers) - 1))
-          wcnt[d[k] * WP + warp] = (CNT)(c + __popc(peers));
+        if (d[k] != kSentinel) wcnt[d[k] * WP + warp] = (CNT)(c + __popc(peers));
         __syncwarp();
       }
     }
@@ -824,7 +823,7 @@ __global__ void __launch_bounds__(THREADS, 1)
       const uint32_t c = valid ? *cp : 0u;
       r[k] = c + __popc(peers & lt);
       __syncwarp();
-      if (valid && lane == (uint32_t)(__ffs(peers) - 1)) *cp = c + __popc(peers);
+      if (valid) *cp = c + __popc(peers);  // every peer writes the same count
       __syncwarp();
     }
     __syncthreads();

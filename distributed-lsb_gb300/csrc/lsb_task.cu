@@ -197,7 +197,7 @@ __device__ __forceinline__ void block_rank8(const uint32_t (&key8)[K], uint32_t 
     const uint32_t c = cnt[key8[k] * WP + warp];
     r[k] = c + __popc(peers & lt);
     __syncwarp();
-    if (lane == (uint32_t)(__ffs(peers) - 1)) cnt[key8[k] * WP + warp] = c + __popc(peers);
+    cnt[key8[k] * WP + warp] = c + __popc(peers);  // every peer writes the same count
     __syncwarp();
   }
   __syncthreads();
