@@ -182,6 +182,12 @@ __device__ __forceinline__ bool pass_skipped(const Ctrl* ctrl, int pass) {
 // ---------------------------------------------------------------------------
 // the onesweep scatter
 
+// Ring slot of tile j: with one slot per tile (the usual layout) the slot is
+// j itself, and the integer division of the general case is skipped.
+__device__ __forceinline__ uint32_t ring_slot(uint32_t j, uint32_t ring_tiles) {
+  return j < ring_tiles ? j : j % ring_tiles;
+}
+
 // Waits until the 64-bit status word at p carries `tag` and a flag; returns
 // it, or returns 0 after kSpinLimit polls (and records the timeout). Once any
 // wait of this launch has failed (ctrl->error set), every later wait returns
@@ -227,7 +233,7 @@ __device__ __forceinline__ uint32_t lookback_digit(const uint64_t* __restrict__ 
     uint64_t s[WN];
 #pragma unroll
     for (int q = 0; q < WN; q++)
-      if (q < cnt) s[q] = ld_relaxed_u64(ring + (size_t)((uint32_t)(j - q) % ring_tiles) * nbins + b);
+      if (q < cnt) s[q] = ld_relaxed_u64(ring + (size_t)ring_slot((uint32_t)(j - q), ring_tiles) * nbins + b);
     *steps += 1;
     int q = 0;
     bool incl = false;
@@ -274,7 +280,7 @@ __device__ __forceinline__ uint32_t walk_one(const uint64_t* __restrict__ ring, 
   uint32_t excl = 0, polls = 0, ns = 8;
   uint32_t j = t - 1;
   for (;;) {
-    const uint64_t e = ld_relaxed_u64(ring + (size_t)(j % ring_tiles) * nbins + b);
+    const uint64_t e = ld_relaxed_u64(ring + (size_t)ring_slot(j, ring_tiles) * nbins + b);
     *steps += 1;
     if (status_tag(e) == ring_tag(pass, j) && status_flag(e) != 0) {
       excl += (uint32_t)e;
@@ -328,7 +334,7 @@ __device__ __forceinline__ void lookback_bins(const uint64_t* __restrict__ ring,
 #pragma unroll
     for (int i = 0; i < NB; i++)
       if (live[i])
-        s[i] = ld_relaxed_u64(ring + (size_t)((uint32_t)j[i] % ring_tiles) * nbins + b0 +
+        s[i] = ld_relaxed_u64(ring + (size_t)ring_slot((uint32_t)j[i], ring_tiles) * nbins + b0 +
                               (uint32_t)i * stride);
     *steps += 1;
     bool moved = false;
@@ -485,7 +491,7 @@ __global__ void __launch_bounds__(THREADS, MINB)
     const TileInfo ti = tile_info(t);
     const uint32_t tile_len = ti.len;
     const bool full = tile_len == E;  // every item valid: no sentinel tests
-    const uint32_t slot = t % ring_tiles;
+    const uint32_t slot = ring_slot(t, ring_tiles);
     const uint32_t tag = ring_tag(pass, t);
     uint32_t* err = &s_err[iter & 1u];
 
@@ -830,7 +836,7 @@ __global__ void __launch_bounds__(THREADS, 1)
 
     // 3. publish the tile's digit counts (after making sure the ring slot's
     //    previous tile has no readers left)
-    const uint32_t slot = t % ring_tiles;
+    const uint32_t slot = ring_slot(t, ring_tiles);
     const uint32_t tag = ring_tag(pass, t);
     bool timed_out = false;
     if (t >= ring_tiles) {
