@@ -240,6 +240,24 @@ __device__ __forceinline__ uint64_t pack_status(uint64_t flag, uint32_t tag, uin
 __device__ __forceinline__ uint32_t status_tag(uint64_t s) { return (uint32_t)(s >> 32) & 0x3FFFFFFFu; }
 __device__ __forceinline__ uint64_t status_flag(uint64_t s) { return s & (3ull << 62); }
 
+// Look-back status word with reach (rings with one slot per tile, where a slot
+// never holds another tile of the same pass, so no tile tag is needed):
+// [63:57] pass + 1, [56:55] flag, [54:32] reach, [31:0] count.
+// Flag kReachPartial: count = the bin's elements in tiles [tile - reach, tile]
+// (reach 0 = the tile's own count, published first; a tile republishes it as
+// its own walk consumes predecessors, so that later tiles jump over what it
+// has covered). Flag kReachIncl: count = the bin's elements in [0, tile].
+constexpr uint32_t kReachPartial = 1u;
+constexpr uint32_t kReachIncl = 2u;
+__device__ __forceinline__ uint64_t pack_reach(uint32_t flag, int pass, uint32_t reach,
+                                               uint32_t count) {
+  return ((uint64_t)(uint32_t)(pass + 1) << 57) | ((uint64_t)flag << 55) |
+         ((uint64_t)(reach & 0x7FFFFFu) << 32) | count;
+}
+__device__ __forceinline__ uint32_t reach_pass(uint64_t s) { return (uint32_t)(s >> 57); }
+__device__ __forceinline__ uint32_t reach_flag(uint64_t s) { return (uint32_t)(s >> 55) & 3u; }
+__device__ __forceinline__ uint32_t reach_span(uint64_t s) { return (uint32_t)(s >> 32) & 0x7FFFFFu; }
+
 // Exclusive block-wide scan of one uint32 per thread. `warp_tot` is a shared
 // array of 33 entries. Returns the exclusive prefix and
 // writes the block total to *total (all threads).

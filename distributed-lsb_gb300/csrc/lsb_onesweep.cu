@@ -207,64 +207,6 @@ __device__ __forceinline__ uint64_t wait_status(const uint64_t* p, uint32_t tag,
   return 0;
 }
 
-// Sums the look-back of digit `b` for tile t: walks predecessors t-1, t-2, ...
-// WN status words at a time (independent loads), adding aggregates until an
-// inclusive prefix is found. Returns the number of digit-b elements in tiles
-// [0, t). Bounded: a predecessor that stays unpublished for kSpinLimit polls
-// (or an error raised elsewhere) ends the walk with *timed_out set.
-// Used where a thread has several bins (wide digits), whose walks run one
-// after another: there a window of 8 measured faster than one word per round.
-constexpr int kLookbackWindow = 8;
-// wide digits: walk a thread's bins interleaved, one word per bin per round
-// (true), or one bin after another with the window above (false)
-constexpr bool kWideInterleaved = true;
-
-template <int WN>
-__device__ __forceinline__ uint32_t lookback_digit(const uint64_t* __restrict__ ring,
-                                                   uint32_t ring_tiles, uint32_t nbins, uint32_t b,
-                                                   int pass, uint32_t t, Ctrl* ctrl,
-                                                   bool* timed_out, uint32_t* steps,
-                                                   uint32_t* polls_out) {
-  uint32_t excl = 0;
-  int64_t j = (int64_t)t - 1;
-  uint32_t polls = 0, ns = 8;
-  while (j >= 0) {
-    const int cnt = j >= WN - 1 ? WN : (int)j + 1;
-    uint64_t s[WN];
-#pragma unroll
-    for (int q = 0; q < WN; q++)
-      if (q < cnt) s[q] = ld_relaxed_u64(ring + (size_t)ring_slot((uint32_t)(j - q), ring_tiles) * nbins + b);
-    *steps += 1;
-    int q = 0;
-    bool incl = false;
-#pragma unroll
-    for (int u = 0; u < WN; u++) {
-      if (u == q && q < cnt) {
-        const uint64_t e = s[u];
-        if (status_tag(e) == ring_tag(pass, (uint32_t)(j - u)) && status_flag(e) != 0) {
-          excl += (uint32_t)e;
-          q++;
-          if (status_flag(e) == kFlagIncl) incl = true;
-        }
-      }
-      if (incl) break;
-    }
-    if (incl) break;
-    j -= q;
-    if (q < cnt) {  // the nearest unconsumed predecessor has not published yet
-      if (++polls >= kSpinLimit || ((polls & 63u) == 0u && error_raised(ctrl))) {
-        record_error(ctrl, kStatusTimeout, kWhereLookback);
-        *timed_out = true;
-        break;
-      }
-      __nanosleep(ns);
-      if (ns < 256) ns <<= 1;
-    }
-  }
-  *polls_out += polls;
-  return excl;
-}
-
 // Decoupled look-back of bin b for tile t: walks predecessors t-1, t-2, ...
 // one status word per round, adding aggregates until it meets an inclusive
 // prefix; returns the number of bin-b elements in tiles [0, t). One status
@@ -286,6 +228,45 @@ __device__ __forceinline__ uint32_t walk_one(const uint64_t* __restrict__ ring, 
       excl += (uint32_t)e;
       if (status_flag(e) == kFlagIncl || j == 0) break;
       j--;
+      ns = 8;
+      continue;
+    }
+    if (++polls >= kSpinLimit || ((polls & 63u) == 0u && error_raised(ctrl))) {
+      record_error(ctrl, kStatusTimeout, kWhereLookback);
+      *timed_out = true;
+      break;
+    }
+    __nanosleep(ns);
+    if (ns < 256) ns <<= 1;
+  }
+  *polls_out += polls;
+  return excl;
+}
+
+// The same walk over statuses with reach (one ring slot per tile): a
+// predecessor's partial status covers the tiles its own walk has consumed,
+// so the walk jumps past all of them in one step, and after every step this
+// tile republishes its own partial status (count so far plus its own count,
+// reach back to the oldest tile consumed) for the tiles walking behind it.
+// Returns the number of bin-b elements in tiles [0, t); publishes nothing
+// final (the caller publishes the inclusive status). Bounded like walk_one.
+__device__ __forceinline__ uint32_t walk_reach(const uint64_t* __restrict__ ring, uint32_t nbins,
+                                               uint32_t b, int pass, uint32_t t, uint32_t own,
+                                               uint64_t* mine, Ctrl* ctrl, bool* timed_out,
+                                               uint32_t* steps, uint32_t* polls_out) {
+  uint32_t excl = 0, polls = 0, ns = 8;
+  uint32_t j = t - 1;
+  const uint32_t want = (uint32_t)pass + 1u;
+  for (;;) {
+    const uint64_t e = ld_relaxed_u64(ring + (size_t)j * nbins + b);
+    *steps += 1;
+    const uint32_t f = reach_flag(e);
+    if (reach_pass(e) == want && f != 0u) {
+      excl += (uint32_t)e;
+      const uint32_t span = reach_span(e);
+      if (f == kReachIncl || j <= span) break;  // j <= span: reached tile 0 (never partial)
+      j -= span + 1u;
+      st_relaxed_u64(mine + b, pack_reach(kReachPartial, pass, t - (j + 1u), excl + own));
       ns = 8;
       continue;
     }
@@ -426,6 +407,9 @@ __global__ void __launch_bounds__(THREADS, MINB)
   Elem* __restrict__ dst = par ? X : Y;
   const bool segmented = seg.tile_seg != nullptr;
   const uint32_t num_tiles = segmented ? *seg.num_tiles : (n + E - 1) / E;
+  // statuses with reach when every tile of the pass has its own ring slot and
+  // each bin has its own walking thread; tile-tagged statuses otherwise
+  const bool reach = ring_tiles >= num_tiles && nbins <= (uint32_t)THREADS;
   const uint32_t warp = threadIdx.x >> 5, lane = lane_id();
   const uint32_t lt = lanemask_lt();
   // bins per thread in the scan: thread i owns bins [i*bpt, i*bpt + bpt)
@@ -589,7 +573,8 @@ __global__ void __launch_bounds__(THREADS, MINB)
 #pragma unroll
         for (int w = 0; w < W; w++) c += wcnt[b * WP + w];
         tcount[b] = c;
-        st_relaxed_u64(my + b, pack_status(ti.first ? kFlagIncl : kFlagAgg, tag, c));
+        st_relaxed_u64(my + b, reach ? pack_reach(ti.first ? kReachIncl : kReachPartial, pass, 0u, c)
+                                     : pack_status(ti.first ? kFlagIncl : kFlagAgg, tag, c));
         sum += c;
       }
       // exclusive scan of `sum` over the CTA (bins are owned in thread order)
@@ -636,27 +621,20 @@ __global__ void __launch_bounds__(THREADS, MINB)
 #pragma unroll
       for (int i = 0; i < NB; i++) excl[i] = 0;
       if (!ti.first && nbins <= (uint32_t)THREADS) {
-        if (threadIdx.x < nbins) {
+        if (threadIdx.x < nbins && reach) {
+          const uint32_t own = tcount[threadIdx.x];
+          excl[0] = walk_reach(ring, nbins, threadIdx.x, pass, t, own, my, ctrl, &timed_out,
+                               &lb_steps, &lb_polls);
+          st_relaxed_u64(my + threadIdx.x, pack_reach(kReachIncl, pass, 0u, excl[0] + own));
+        } else if (threadIdx.x < nbins) {
           excl[0] = walk_one(ring, ring_tiles, nbins, threadIdx.x, pass, t, ctrl, &timed_out,
                              &lb_steps, &lb_polls);
           st_relaxed_u64(my + threadIdx.x,
                          pack_status(kFlagIncl, tag, excl[0] + tcount[threadIdx.x]));
         }
-      } else if (!ti.first && kWideInterleaved) {
+      } else if (!ti.first) {  // several bins per thread (wide digits): walks interleaved
         lookback_bins<NB>(ring, ring_tiles, nbins, threadIdx.x, THREADS, pass, t, excl, my, tag,
                           tcount, ctrl, &timed_out, &lb_steps, &lb_polls);
-      } else if (!ti.first) {
-        // several bins per thread: each bin's inclusive prefix is published
-        // as soon as its walk ends (later tiles' walks stop there)
-#pragma unroll
-        for (int i = 0; i < NB; i++) {
-          const uint32_t b = threadIdx.x + (uint32_t)i * THREADS;
-          if (b < nbins) {
-            excl[i] = lookback_digit<kLookbackWindow>(ring, ring_tiles, nbins, b, pass, t, ctrl,
-                                                      &timed_out, &lb_steps, &lb_polls);
-            st_relaxed_u64(my + b, pack_status(kFlagIncl, tag, excl[i] + tcount[b]));
-          }
-        }
       }
 #pragma unroll
       for (int i = 0; i < NB; i++) {
