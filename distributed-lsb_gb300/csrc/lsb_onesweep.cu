@@ -363,9 +363,8 @@ __device__ __forceinline__ void lookback_bins(const uint64_t* __restrict__ ring,
 //   2. stable rank inside each warp (ballot peers, per-warp counters);
 //   3. per-bin row sums, published at once (so that later tiles can use
 //      them), scan of the bin totals, per-(bin, warp) starts written back;
-//   4. stage the tile in digit order;
-//   5. decoupled look-back per bin -> global start of each bin; issue the
-//      next tile's loads;
+//   4. decoupled look-back per bin -> global start of each bin;
+//   5. stage the tile in digit order; issue the next tile's loads;
 //   6. the stores: up to 256 bins one bulk copy (shared -> global, async
 //      proxy) per run of equal digits, which drains while the next tile is
 //      ranked; above, 16-byte stores by every thread.
@@ -602,18 +601,14 @@ __global__ void __launch_bounds__(THREADS, MINB)
       }
     }
     __syncthreads();
-    // 4. stage this thread's items in digit order (made visible to the bulk
-    //    copies); up to 256 bins each warp then clears its own counter column
-#pragma unroll
-    for (int k = 0; k < K; k++)
-      if (full || d[k] != kSentinel) stage[r[k] + wcnt[d[k] * WP + warp]] = v[k];
-    fence_proxy_async_smem();
-    if (column_clear) {
-      __syncwarp();
-      for (uint32_t b = lane; b < nbins; b += 32u) wcnt[b * WP + warp] = 0;
-    }
-    // 5. decoupled look-back of this thread's bins b = threadIdx.x + i x THREADS
-    {
+    // 4. decoupled look-back of this thread's bins b = threadIdx.x + i x THREADS;
+    // 5. stage this thread's items in digit order (made visible to the bulk
+    //    copies); up to 256 bins each warp then clears its own counter column.
+    //    With statuses that carry reach (one bin per thread) the walk runs
+    //    before the staging, which publishes this tile's inclusive counts
+    //    sooner (measured faster); with tile-tagged statuses it runs after
+    //    (measured faster there).
+    auto lookback = [&]() {
       constexpr int NB = (BITS > 0 ? (1 << BITS) : (1 << kMaxOnesweepBits)) / THREADS > 0
                              ? (BITS > 0 ? (1 << BITS) : (1 << kMaxOnesweepBits)) / THREADS
                              : 1;
@@ -641,6 +636,23 @@ __global__ void __launch_bounds__(THREADS, MINB)
         const uint32_t b = threadIdx.x + (uint32_t)i * THREADS;
         if (b < nbins) gbase[b] = ti.seg_base + ti.gs[b] + excl[i];
       }
+    };
+    auto stage_tile = [&]() {
+#pragma unroll
+      for (int k = 0; k < K; k++)
+        if (full || d[k] != kSentinel) stage[r[k] + wcnt[d[k] * WP + warp]] = v[k];
+      fence_proxy_async_smem();
+      if (column_clear) {
+        __syncwarp();
+        for (uint32_t b = lane; b < nbins; b += 32u) wcnt[b * WP + warp] = 0;
+      }
+    };
+    if (reach && nbins <= (uint32_t)THREADS) {
+      lookback();
+      stage_tile();
+    } else {
+      stage_tile();
+      lookback();
     }
     // the next tile's loads, into the registers freed by the staging (issued
     // after the look-back: loads in flight slow the look-back's own loads)
