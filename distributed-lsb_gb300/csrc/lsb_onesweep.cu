@@ -604,10 +604,12 @@ __global__ void __launch_bounds__(THREADS, MINB)
     // 4. decoupled look-back of this thread's bins b = threadIdx.x + i x THREADS;
     // 5. stage this thread's items in digit order (made visible to the bulk
     //    copies); up to 256 bins each warp then clears its own counter column.
-    //    With statuses that carry reach (one bin per thread) the walk runs
-    //    before the staging, which publishes this tile's inclusive counts
-    //    sooner (measured faster); with tile-tagged statuses it runs after
-    //    (measured faster there).
+    //    With statuses that carry reach and at most one bin per two threads
+    //    (8-bit digits on 512 threads) the walk runs before the staging,
+    //    which publishes this tile's inclusive counts sooner; otherwise it
+    //    runs after. Each order measured faster where it is used (on 256
+    //    threads with a bin each, walking first polled unpublished
+    //    predecessors far more often).
     auto lookback = [&]() {
       constexpr int NB = (BITS > 0 ? (1 << BITS) : (1 << kMaxOnesweepBits)) / THREADS > 0
                              ? (BITS > 0 ? (1 << BITS) : (1 << kMaxOnesweepBits)) / THREADS
@@ -647,7 +649,7 @@ __global__ void __launch_bounds__(THREADS, MINB)
         for (uint32_t b = lane; b < nbins; b += 32u) wcnt[b * WP + warp] = 0;
       }
     };
-    if (reach && nbins <= (uint32_t)THREADS) {
+    if (reach && 2u * nbins <= (uint32_t)THREADS) {
       lookback();
       stage_tile();
     } else {
@@ -936,7 +938,7 @@ __global__ void __launch_bounds__(THREADS, 1)
 // tiles, one CTA per SM), 32-bit counters up to 256 digits, 16-bit above.
 // LSB_ONESWEEP_VARIANT selects another shape (a tuning knob; measured on
 // GB300 at 2^30 elements, 16-bit digits as eight 8-bit passes, per sort:
-// 0 -> 76.9 ms, 2 -> 87.0 ms, 1 -> 102.9 ms; 3 was the slowest when last
+// 0 -> 59.0 ms, 2 -> 67.7 ms, 1 -> 97.6 ms; 3 was the slowest when last
 // measured):
 //  1: bulk-copy kernel 768 x 8 (6144-element tiles, 24 warps) up to 256 digits;
 //  2: register kernel 256 x 16, two CTAs per SM;
