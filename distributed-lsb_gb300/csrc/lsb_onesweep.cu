@@ -9,8 +9,8 @@
 // dispatched in input order; each tile ranks its keys in shared memory,
 // learns the number of earlier elements of each digit from its predecessors
 // by decoupled look-back (replacing the count all-to-all and Exscan), stages
-// the tile in digit order in shared memory and writes runs of equal digits
-// with coalesced 16-byte stores.
+// the tile in digit order in shared memory and writes each run of equal
+// digits with one bulk copy (16-byte stores for more than 256 digits).
 #include <algorithm>
 #include <cstdlib>
 
@@ -363,7 +363,8 @@ __device__ __forceinline__ void lookback_bins(const uint64_t* __restrict__ ring,
 //   2. stable rank inside each warp (ballot peers, per-warp counters);
 //   3. per-bin row sums, published at once (so that later tiles can use
 //      them), scan of the bin totals, per-(bin, warp) starts written back;
-//   4. decoupled look-back per bin -> global start of each bin;
+//   4. decoupled look-back per bin -> global start of each bin (after step 5
+//      where statuses are tile-tagged or a bin has one thread);
 //   5. stage the tile in digit order; issue the next tile's loads;
 //   6. the stores: up to 256 bins one bulk copy (shared -> global, async
 //      proxy) per run of equal digits, which drains while the next tile is
