@@ -35,10 +35,12 @@ def _existing(lsb, torch, a: np.ndarray, bits: int) -> np.ndarray:
 
 
 def test_noalloc_matches_sort_pairs_twice_in_a_row(lsb, cuda, oracle):
-    # large enough that the look-back ring wraps (tiles > ring slots), and a
-    # smaller second call that must not see the first call's ring entries
-    cases = [((1 << 22) + 3, oracle.DIST_UNIFORM, 8), (70001, oracle.DIST_ZIPF, 8),
-             ((1 << 22) + 3, oracle.DIST_NEARLY_SORTED, 5), (4097, oracle.DIST_LOW32, 8)]
+    # large enough that the look-back ring wraps (1025 tiles of 8192 elements,
+    # more than the fixed scratch's ring slots: slot reuse, completion tags,
+    # tile-tagged statuses), and a smaller second call that must not see the
+    # first call's ring entries
+    cases = [((1 << 23) + 3, oracle.DIST_UNIFORM, 8), (70001, oracle.DIST_ZIPF, 8),
+             ((1 << 23) + 3, oracle.DIST_NEARLY_SORTED, 5), (4097, oracle.DIST_LOW32, 8)]
     for call in range(2):
         for n, dist, bits in cases:
             a = oracle.generate(n, dist, seed=100 + call)
