@@ -188,25 +188,6 @@ __device__ __forceinline__ uint32_t ring_slot(uint32_t j, uint32_t ring_tiles) {
   return j < ring_tiles ? j : j % ring_tiles;
 }
 
-// Waits until the 64-bit status word at p carries `tag` and a flag; returns
-// it, or returns 0 after kSpinLimit polls (and records the timeout). Once any
-// wait of this launch has failed (ctrl->error set), every later wait returns
-// at once, so a failure costs one spin limit, not one per tile and digit.
-__device__ __forceinline__ uint64_t wait_status(const uint64_t* p, uint32_t tag, Ctrl* ctrl,
-                                                bool* timed_out) {
-  uint32_t ns = 8;
-  for (uint32_t it = 0; it < kSpinLimit; it++) {
-    const uint64_t s = ld_relaxed_u64(p);
-    if (status_tag(s) == tag && status_flag(s) != 0) return s;
-    if ((it & 63u) == 0u && error_raised(ctrl)) break;
-    __nanosleep(ns);
-    if (ns < 256) ns <<= 1;
-  }
-  record_error(ctrl, kStatusTimeout, kWhereLookback);
-  *timed_out = true;
-  return 0;
-}
-
 // Decoupled look-back of bin b for tile t: walks predecessors t-1, t-2, ...
 // one status word per round, adding aggregates until it meets an inclusive
 // prefix; returns the number of bin-b elements in tiles [0, t). One status
