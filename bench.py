@@ -5,9 +5,10 @@ Workload (the headline configuration): one step = one full LSD sort
 (lsb_sort_pairs, the reference's mySort, mpi/mpi_lsbsort.cpp:592-597) of
 2^30 16-byte {uint64 key, uint64 value} elements, keys uniform from the seeded
 splitmix64 stream, value = index, 16-bit digits (the reference's RADIX, 4
-passes). The input is restored from a resident copy before every step (not
-timed), so every step sorts the same unsorted 16 GiB array; arrays are far
-larger than L2, and the restore copy itself sweeps L2.
+digits, each run as two stable 8-bit sub-passes). The input is restored from
+a resident copy before every step (not timed), so every step sorts the same
+unsorted 16 GiB array; arrays are far larger than L2, and the restore copy
+itself sweeps L2.
 
 Prints ONE JSON line (rank 0):
   value        M elements/s, whole job, inputs resident in HBM, CUDA events
@@ -18,6 +19,10 @@ Prints ONE JSON line (rank 0):
   cpu_baseline the oracle's port of the reference algorithm on the host cores
                (bounded sample), rank 0 at N=1 only
   clocks       SM clock samples taken during the timed region
+  segmented    4096 arrays of floor(2^U(10,22)) elements: one batched,
+               graph-captured sort against a loop of lsb_sort_pairs
+  serving      10^4 Poisson-arrival requests through the request loop:
+               latency p50/p99 and elements/s
 
 --impl reference times the reference algorithm on the host cores instead
 (see cpu_arm below). --gpus N (torchrun) runs N independent replicas, one
