@@ -107,16 +107,36 @@ class DeviceArray {
 };
 
 // One pass over `digit`: afterwards A holds the elements stably sorted by
-// that digit and B is scratch -- the contract of globalShuffle. The pass
-// writes into B and the two arrays then trade buffers, which is the same
-// observable result without a copy back.
+// that digit and B is scratch -- the contract of globalShuffle. A wide even
+// digit (12, 14, 16 bits) runs as two stable half-width passes, A -> B by its
+// low half and B -> A by its high half: a stable sort by the low half followed
+// by a stable sort by the high half is the stable sort by the whole digit, and
+// the half-width passes run on the faster kernel family. Otherwise (or when
+// the high half lies wholly above bit 63) one pass writes B and the two arrays
+// trade buffers, the same observable result without a copy back.
 inline void globalShuffle(DeviceArray<SortElement>& A, DeviceArray<SortElement>& B, int digit,
                           int digitBits = 16) {
   if (A.numElementsTotal() != B.numElementsTotal())
     throw Error(LSB_ERR_INVALID_ARG, "globalShuffle: A and B differ in size");
-  check(lsb_pass(reinterpret_cast<const lsb_elem_t*>(A.data()), reinterpret_cast<lsb_elem_t*>(B.data()),
-                 A.numElementsTotal(), digitBits, digit, nullptr, 0, nullptr),
-        "lsb_pass");
+  const int64_t n = A.numElementsTotal();
+  auto pass = [&](const SortElement* src, SortElement* dst, int bits, int d) {
+    check(lsb_pass(reinterpret_cast<const lsb_elem_t*>(src), reinterpret_cast<lsb_elem_t*>(dst), n,
+                   bits, d, nullptr, 0, nullptr),
+          "lsb_pass");
+  };
+  const int half = digitBits / 2;
+  const bool split = digitBits > 11 && digitBits % 2 == 0 && digit >= 0 &&
+                     digit < lsb_num_passes(digitBits);
+  if (split && (2 * digit + 1) * half < 64) {
+    pass(A.data(), B.data(), half, 2 * digit);
+    pass(B.data(), A.data(), half, 2 * digit + 1);
+    return;
+  }
+  if (split) {
+    pass(A.data(), B.data(), half, 2 * digit);
+  } else {
+    pass(A.data(), B.data(), digitBits, digit);
+  }
   A.swapStorage(B);
 }
 

@@ -5,7 +5,9 @@
 //
 // Extra flags: --digit-bits B (8, 11 or 16; the reference's RADIX is 16),
 // --dist NAME (uniform, low32, zipf, equal, nearly_sorted), --seed S,
-// --warmup W (untimed sorts of a copy of the input before the timed one).
+// --warmup W (untimed sorts of a copy of the input before the timed one),
+// --per-pass (sort by a loop of globalShuffle over the digits, the structure
+// of the reference's mySort, instead of one lsb_sort_pairs call).
 //
 // Input: key from the seeded splitmix64 stream, value = global index, like
 // the reference's pcg64(rank) generator with val = global index (:686-692).
@@ -58,6 +60,7 @@ int main(int argc, char** argv) {
   int64_t n = 100 * 1000 * 1000;
   int digitBits = 16, dist = LSB_DIST_UNIFORM, warmup = 1;
   uint64_t seed = 0;
+  bool perPass = false;  // sort by a loop of globalShuffle, the reference's own mySort
   for (int i = 1; i < argc; i++) {
     std::string a = argv[i];
     auto next = [&]() -> std::string {
@@ -74,6 +77,7 @@ int main(int argc, char** argv) {
     else if (a == "--digit-bits") digitBits = std::stoi(next());
     else if (a == "--seed") seed = std::stoull(next());
     else if (a == "--warmup") warmup = std::stoi(next());
+    else if (a == "--per-pass") perPass = true;
     else if (a == "--dist") {
       std::string d = next();
       if (d == "uniform") dist = LSB_DIST_UNIFORM;
@@ -112,8 +116,16 @@ int main(int argc, char** argv) {
                                      cudaMemcpyDeviceToDevice), "copy input");
     if (verifyLocally) In.copyToHost(LocalInputCopy);
 
+    auto sort = [&]() {
+      if (perPass) {
+        for (int digit = 0; digit < lsb_num_passes(digitBits); digit++)
+          lsb_gb300::globalShuffle(A, B, digit, digitBits);
+      } else {
+        lsb_gb300::mySort(A, B, digitBits);
+      }
+    };
     for (int w = 0; w < warmup; w++) {
-      lsb_gb300::mySort(A, B, digitBits);
+      sort();
       lsb_gb300::check_cuda(cudaMemcpy(A.data(), In.data(), sizeof(SortElement) * (size_t)n,
                                        cudaMemcpyDeviceToDevice), "restore input");
     }
@@ -124,7 +136,7 @@ int main(int argc, char** argv) {
     cudaEventCreate(&e1);
     lsb_gb300::check_cuda(cudaDeviceSynchronize(), "sync");
     cudaEventRecord(e0);
-    lsb_gb300::mySort(A, B, digitBits);
+    sort();
     cudaEventRecord(e1);
     lsb_gb300::check_cuda(cudaEventSynchronize(e1), "sort");
     float ms = 0.f;

@@ -162,8 +162,10 @@ def test_cpp_driver_runs_and_verifies(lsb, cuda):
 
     from lsb_gb300 import _build
 
-    for bits, dist in ((16, "uniform"), (8, "zipf"), (11, "nearly_sorted")):
+    for bits, dist, per_pass in ((16, "uniform", False), (8, "zipf", False), (11, "nearly_sorted", False),
+                                 (16, "uniform", True), (12, "zipf", True), (11, "low32", True)):
+        extra = ["--per-pass"] if per_pass else []
         r = subprocess.run([_build.DRIVER_PATH, "--n", "300001", "--digit-bits", str(bits), "--dist", dist,
-                            "--verify"], capture_output=True, text=True, timeout=300)
+                            "--verify", *extra], capture_output=True, text=True, timeout=300)
         assert r.returncode == 0, r.stdout + r.stderr
         assert "Verification passed" in r.stdout and "Device check: 0 violations" in r.stdout
