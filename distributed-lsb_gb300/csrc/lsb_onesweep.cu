@@ -344,8 +344,9 @@ __device__ __forceinline__ void lookback_bins(const uint64_t* __restrict__ ring,
 //   2. stable rank inside each warp (ballot peers, per-warp counters);
 //   3. per-bin row sums, published at once (so that later tiles can use
 //      them), scan of the bin totals, per-(bin, warp) starts written back;
-//   4. decoupled look-back per bin -> global start of each bin (after step 5
-//      where statuses are tile-tagged or a bin has one thread);
+//   4. decoupled look-back per bin -> global start of each bin (after a
+//      quarter of step 5 where statuses carry reach and a bin has two
+//      threads, after all of step 5 otherwise);
 //   5. stage the tile in digit order; issue the next tile's loads;
 //   6. the stores: up to 256 bins one bulk copy (shared -> global, async
 //      proxy) per run of equal digits, which drains while the next tile is
@@ -587,11 +588,13 @@ __global__ void __launch_bounds__(THREADS, MINB)
     // 5. stage this thread's items in digit order (made visible to the bulk
     //    copies); up to 256 bins each warp then clears its own counter column.
     //    With statuses that carry reach and at most one bin per two threads
-    //    (8-bit digits on 512 threads) the walk runs before the staging,
-    //    which publishes this tile's inclusive counts sooner; otherwise it
-    //    runs after. Each order measured faster where it is used (on 256
-    //    threads with a bin each, walking first polled unpublished
-    //    predecessors far more often).
+    //    (8-bit digits on 512 threads) the walk runs after a quarter of the
+    //    items is staged and before the rest, which publishes this tile's
+    //    inclusive counts sooner while giving the nearest predecessors a
+    //    moment to publish theirs; otherwise it runs after the staging. Each
+    //    order measured fastest where it is used (walking at once polled
+    //    unpublished predecessors far more often, and on 256 threads with a
+    //    bin each walking first at all did).
     auto lookback = [&]() {
       constexpr int NB = (BITS > 0 ? (1 << BITS) : (1 << kMaxOnesweepBits)) / THREADS > 0
                              ? (BITS > 0 ? (1 << BITS) : (1 << kMaxOnesweepBits)) / THREADS
@@ -621,19 +624,27 @@ __global__ void __launch_bounds__(THREADS, MINB)
         if (b < nbins) gbase[b] = ti.seg_base + ti.gs[b] + excl[i];
       }
     };
-    auto stage_tile = [&]() {
+    auto stage_part = [&](int k0, int k1) {
 #pragma unroll
       for (int k = 0; k < K; k++)
-        if (full || d[k] != kSentinel) stage[r[k] + wcnt[d[k] * WP + warp]] = v[k];
+        if (k >= k0 && k < k1 && (full || d[k] != kSentinel)) stage[r[k] + wcnt[d[k] * WP + warp]] = v[k];
+    };
+    auto stage_done = [&]() {
       fence_proxy_async_smem();
       if (column_clear) {
         __syncwarp();
         for (uint32_t b = lane; b < nbins; b += 32u) wcnt[b * WP + warp] = 0;
       }
     };
+    auto stage_tile = [&]() {
+      stage_part(0, K);
+      stage_done();
+    };
     if (reach && 2u * nbins <= (uint32_t)THREADS) {
+      stage_part(0, K / 4);
       lookback();
-      stage_tile();
+      stage_part(K / 4, K);
+      stage_done();
     } else {
       stage_tile();
       lookback();
