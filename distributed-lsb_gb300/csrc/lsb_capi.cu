@@ -75,7 +75,7 @@ int current_device_info(DeviceInfo* info) {
   return 0;
 }
 
-static int pool_alloc(void** ptr, size_t bytes, cudaStream_t st) {
+int pool_alloc(void** ptr, size_t bytes, cudaStream_t st) {
   cudaMemPool_t pool = device_pool();
   if (!pool) return LSB_ERR_NO_DEVICE;
   if (bytes == 0) bytes = 256;
@@ -500,6 +500,8 @@ int lsb_sort_pairs_host(lsb_elem_t* h_a, int64_t n, int digit_bits, void* stream
   if (n > LSB_MAX_ELEMENTS) return LSB_ERR_TOO_LARGE;
   if (n <= 1) return LSB_OK;
   cudaStream_t st = (cudaStream_t)stream;
+  const int chunks = host_chunks(n);
+  if (chunks > 1) return host_sort_pipelined(reinterpret_cast<Elem*>(h_a), n, digit_bits, chunks, st);
   Layout L;
   if (int rc = plan_layout(n, digit_bits, lsb_num_passes(digit_bits), &L, true)) return rc;
   const size_t bytes = (size_t)n * sizeof(Elem);

@@ -100,6 +100,16 @@ int final_copy(Elem* X, Elem* Y, uint32_t n, int num_digits, int target_parity, 
 
 inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
+// Stream-ordered allocation from the library's per-device pool (freed blocks
+// stay in the pool for later calls). Returns an LSB_ERR_* code.
+int pool_alloc(void** ptr, size_t bytes, cudaStream_t st);
+
+// Host-buffer sort (lsb_host.cu): the number of chunks whose copies overlap
+// the sorts of earlier chunks (1 = copy in, sort, copy out), and the chunked
+// pipeline itself (chunks a power of two >= 2). Blocking; sorts h in place.
+int host_chunks(int64_t n);
+int host_sort_pipelined(Elem* h, int64_t n, int digit_bits, int chunks, cudaStream_t st);
+
 // Profiling scope: when lsb_profile_enable(1) is in effect, records a CUDA
 // event on `st` at construction and another at destruction, under `name`.
 class ProfScope {

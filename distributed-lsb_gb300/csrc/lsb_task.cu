@@ -301,7 +301,7 @@ __global__ void __launch_bounds__(kScatThreads)
       }
       key8[k] = dg[k] & 0xFFu;
     }
-    // round 1: low 8 bits of the digit, in input order
+    // first ranking: low 8 bits of the digit, in input order
     block_rank8<THREADS, K>(key8, r, cnt, wt);
 #pragma unroll
     for (int k = 0; k < K; k++) {
@@ -309,7 +309,7 @@ __global__ void __launch_bounds__(kScatThreads)
       packA[r[k]] = (dg[k] << 16) | s;
     }
     __syncthreads();
-    // round 2: high bits, in round-1 order -> stable sort by the whole digit
+    // second ranking: high bits, in first-ranking order -> stable sort by the whole digit
     uint32_t x[K];
 #pragma unroll
     for (int k = 0; k < K; k++) {

@@ -157,6 +157,35 @@ def test_host_buffer_entry_point(lsb, cuda, oracle):
         assert np.array_equal(t.numpy().view(np.uint64), oracle.stable_sort_by_key(a))
 
 
+@pytest.mark.parametrize("chunks", [2, 4, 8, 16])
+def test_host_buffer_pipeline(lsb, cuda, oracle, monkeypatch, chunks):
+    """The chunked host-buffer sort (copies overlapped with chunk sorts, then
+    stable merges) equals the stable sort: empty and one-element chunks, ties
+    across chunk boundaries (equal keys, Zipf), several output slices."""
+    monkeypatch.setenv("LSB_HOST_CHUNKS", str(chunks))
+    for n, dist, bits in ((5, oracle.DIST_UNIFORM, 16), (17, oracle.DIST_EQUAL, 8),
+                          (300007, oracle.DIST_ZIPF, 16), (300007, oracle.DIST_EQUAL, 11),
+                          ((1 << 21) + 3, oracle.DIST_UNIFORM, 8), ((1 << 21) + 3, oracle.DIST_ZIPF, 13),
+                          ((1 << 21) + 3, oracle.DIST_NEARLY_SORTED, 16)):
+        a = oracle.generate(n, dist, 21)
+        h = a.copy()
+        lsb.sort_pairs_host(h, bits)
+        assert np.array_equal(h, oracle.stable_sort_by_key(a)), (chunks, n, dist, bits)
+    a = oracle.generate(300007, oracle.DIST_LOW32, 5)
+    t = cuda.from_numpy(a.view(np.int64).copy()).pin_memory()
+    lsb.sort_pairs_host(t, 16)
+    assert np.array_equal(t.numpy().view(np.uint64), oracle.stable_sort_by_key(a))
+
+
+def test_host_buffer_pipeline_default_size(lsb, cuda, oracle, monkeypatch):
+    """From 2^25 elements the host-buffer call pipelines by default (8 chunks, 16 slices)."""
+    monkeypatch.delenv("LSB_HOST_CHUNKS", raising=False)
+    a = oracle.generate((1 << 25) + 11, oracle.DIST_ZIPF, 3)
+    t = cuda.from_numpy(a.view(np.int64).copy()).pin_memory()
+    lsb.sort_pairs_host(t, 16)
+    assert np.array_equal(t.numpy().view(np.uint64), oracle.stable_sort_by_key(a))
+
+
 def test_cpp_driver_runs_and_verifies(lsb, cuda):
     import subprocess
 
