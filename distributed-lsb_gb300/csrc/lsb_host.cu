@@ -33,7 +33,7 @@ namespace lsb {
 constexpr int kMergeThreads = 256;
 constexpr int kMergeItems = 8;
 constexpr uint32_t kMergeTile = (uint32_t)kMergeThreads * kMergeItems;  // output elements per tile
-constexpr size_t kMergeSmem = 2u * kMergeTile * sizeof(Elem);           // input tile + output tile
+constexpr size_t kMergeSmem = 3u * kMergeTile * sizeof(Elem);           // two input tiles + output tile
 
 // Number of elements of A among the first d elements of the merge (merge path
 // co-rank), ties going to A: the smallest i with A[i] after B[d-1-i].
@@ -63,43 +63,83 @@ __global__ void k_merge_bounds(const Elem* __restrict__ a, uint32_t na, const El
 // apart across a warp) and the coalesced read-out both hit distinct banks.
 __device__ __forceinline__ uint32_t merge_slot(uint32_t o) { return o ^ ((o >> 3) & 7u); }
 
+// Tile geometry from the co-ranks: first output position t0, length len,
+// A slice [ia0, ia0 + la), B slice [t0 - ia0, ...). False when the co-ranks
+// are not monotone or leave the runs (reported, never followed).
+__device__ __forceinline__ bool merge_tile(const uint32_t* bounds, uint32_t t, uint32_t na, uint32_t nb,
+                                           uint32_t d_lo, uint32_t d_hi, uint32_t& t0, uint32_t& len,
+                                           uint32_t& ia0, uint32_t& la) {
+  const uint64_t t0_64 = (uint64_t)d_lo + (uint64_t)t * kMergeTile;
+  t0 = (uint32_t)t0_64;
+  const uint32_t t1 = t0_64 + kMergeTile < d_hi ? (uint32_t)(t0_64 + kMergeTile) : d_hi;
+  ia0 = bounds[t];
+  const uint32_t ia1 = bounds[t + 1];
+  len = t1 - t0;
+  la = ia1 - ia0;
+  return ia0 <= ia1 && ia1 <= na && ia0 <= t0 && ia1 <= t1 && ia1 - ia0 <= len && t1 - ia1 <= nb &&
+         t0 - ia0 <= t1 - ia1;
+}
+
 // Writes merge positions [d_lo, d_hi) of A and B to out[d_lo .. d_hi), one
-// tile of kMergeTile positions per CTA iteration: the tile's slices of A and B
-// are staged in shared memory, each thread merges kMergeItems consecutive
-// outputs from its own co-rank, and the tile leaves in coalesced 16-byte stores.
+// tile of kMergeTile positions per CTA iteration. The tile's slices of A and
+// B (contiguous in both runs) arrive by two bulk copies into one of two input
+// buffers while the CTA merges the previous tile from the other; each thread
+// merges kMergeItems consecutive outputs from its own co-rank, and the tile
+// leaves in coalesced 16-byte stores.
 __global__ void __launch_bounds__(kMergeThreads)
     k_merge_pair(const Elem* __restrict__ a, uint32_t na, const Elem* __restrict__ b, uint32_t nb,
                  Elem* __restrict__ out, uint32_t d_lo, uint32_t d_hi, uint32_t tiles,
                  const uint32_t* __restrict__ bounds, uint32_t* __restrict__ err) {
-  extern __shared__ __align__(16) unsigned char merge_smem[];
-  Elem* s_in = reinterpret_cast<Elem*>(merge_smem);
-  Elem* s_out = s_in + kMergeTile;
-  for (uint32_t t = blockIdx.x; t < tiles; t += gridDim.x) {
-    const uint64_t t0_64 = (uint64_t)d_lo + (uint64_t)t * kMergeTile;
-    const uint32_t t0 = (uint32_t)t0_64;
-    const uint32_t t1 = t0_64 + kMergeTile < d_hi ? (uint32_t)(t0_64 + kMergeTile) : d_hi;
-    const uint32_t ia0 = bounds[t], ia1 = bounds[t + 1];
-    const uint32_t len = t1 - t0;
-    // co-ranks are monotone and within the runs; anything else is reported, not followed
-    const bool ok = ia0 <= ia1 && ia1 <= na && ia0 <= t0 && ia1 <= t1 && ia1 - ia0 <= len &&
-                    t1 - ia1 <= nb && t0 - ia0 <= t1 - ia1;
-    if (!ok) {
+  extern __shared__ __align__(128) unsigned char merge_smem[];
+  Elem* s_in = reinterpret_cast<Elem*>(merge_smem);  // [2][kMergeTile]
+  Elem* s_out = s_in + 2u * kMergeTile;
+  __shared__ __align__(8) uint64_t s_bar[2];
+  uint32_t phases = 0, pending = 0;  // per input buffer: barrier phase, copy in flight (thread 0)
+  // thread 0: start the copies of tile t into input buffer `buf`
+  auto issue = [&](uint32_t t, uint32_t buf) {
+    uint32_t t0, len, ia0, la;
+    if (!merge_tile(bounds, t, na, nb, d_lo, d_hi, t0, len, ia0, la)) return;
+    const uint32_t bar = smem_u32(&s_bar[buf]);
+    const uint32_t dst = smem_u32(s_in + buf * kMergeTile);
+    fence_proxy_async_smem();  // the buffer's earlier generic reads come first
+    mbar_arrive_expect_tx(bar, len * (uint32_t)sizeof(Elem));
+    if (la) bulk_g2s(dst, a + ia0, la * (uint32_t)sizeof(Elem), bar);
+    if (len > la) bulk_g2s(dst + la * (uint32_t)sizeof(Elem), b + (t0 - ia0), (len - la) * (uint32_t)sizeof(Elem), bar);
+    pending |= 1u << buf;
+  };
+  if (threadIdx.x == 0) {
+    mbar_init(smem_u32(&s_bar[0]), 1);
+    mbar_init(smem_u32(&s_bar[1]), 1);
+    fence_mbar_init();
+    if (blockIdx.x < tiles) issue(blockIdx.x, 0);
+  }
+  __syncthreads();
+  uint32_t k = 0;
+  for (uint32_t t = blockIdx.x; t < tiles; t += gridDim.x, k++) {
+    const uint32_t buf = k & 1u;
+    if (threadIdx.x == 0 && t + gridDim.x < tiles) issue(t + gridDim.x, buf ^ 1u);
+    uint32_t t0, len, ia0, la;
+    if (!merge_tile(bounds, t, na, nb, d_lo, d_hi, t0, len, ia0, la)) {
       if (threadIdx.x == 0) atomicCAS(err, 0u, kStatusInconsistent);
       continue;
     }
-    const uint32_t la = ia1 - ia0, lb = len - la, ib0 = t0 - ia0;
-    for (uint32_t i = threadIdx.x; i < la; i += kMergeThreads) s_in[i] = load_elem_stream(a + ia0 + i);
-    for (uint32_t i = threadIdx.x; i < lb; i += kMergeThreads) s_in[la + i] = load_elem_stream(b + ib0 + i);
-    __syncthreads();
-    const Elem* sa = s_in;
-    const Elem* sb = s_in + la;
+    const bool arrived = mbar_wait_bounded(smem_u32(&s_bar[buf]), (phases >> buf) & 1u);
+    phases ^= 1u << buf;
+    if (__syncthreads_or(!arrived)) {
+      if (threadIdx.x == 0) atomicCAS(err, 0u, kStatusTimeout);
+      break;
+    }
+    if (threadIdx.x == 0) pending &= ~(1u << buf);
+    const uint32_t lb = len - la;
+    const Elem* sa = s_in + buf * kMergeTile;
+    const Elem* sb = sa + la;
     const uint32_t d = min(threadIdx.x * (uint32_t)kMergeItems, len);
     uint32_t i = merge_corank(sa, la, sb, lb, d);
     uint32_t j = d - i;
     Elem ea = sa[min(i, la - (la > 0u))], eb = sb[min(j, lb - (lb > 0u))];
 #pragma unroll
-    for (int k = 0; k < kMergeItems; k++) {
-      const uint32_t o = d + (uint32_t)k;
+    for (int q = 0; q < kMergeItems; q++) {
+      const uint32_t o = d + (uint32_t)q;
       if (o < len) {
         const bool take_a = j >= lb || (i < la && ea.key <= eb.key);
         if (take_a) {
@@ -113,8 +153,12 @@ __global__ void __launch_bounds__(kMergeThreads)
     }
     __syncthreads();
     for (uint32_t o = threadIdx.x; o < len; o += kMergeThreads) store_elem(out + t0 + o, s_out[merge_slot(o)]);
-    __syncthreads();  // the next tile reuses both buffers
+    __syncthreads();  // s_out and this input buffer are reused
   }
+  // leaving after an error: let the copies in flight land before the CTA exits
+  if (threadIdx.x == 0)
+    for (uint32_t q = 0; q < 2u; q++)
+      if (pending & (1u << q)) mbar_wait_bounded(smem_u32(&s_bar[q]), (phases >> q) & 1u);
 }
 
 // Merges positions [d_lo, d_hi) of runs a (na elements, earlier) and b (nb,
@@ -133,7 +177,7 @@ static int merge_pair(const Elem* a, uint32_t na, const Elem* b, uint32_t nb, El
   if (cudaFuncSetAttribute(k_merge_pair, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMergeSmem) !=
       cudaSuccess)
     return LSB_ERR_CUDA;
-  const uint32_t grid = std::max<uint32_t>(1u, std::min<uint32_t>(tiles, (uint32_t)dev.sm_count * 3u));
+  const uint32_t grid = std::max<uint32_t>(1u, std::min<uint32_t>(tiles, (uint32_t)dev.sm_count * 2u));
   ProfScope prof("merge_runs", st);
   k_merge_pair<<<grid, kMergeThreads, kMergeSmem, st>>>(a, na, b, nb, out, d_lo, d_hi, tiles, bounds, err);
   return cudaPeekAtLastError() == cudaSuccess ? 0 : LSB_ERR_CUDA;
@@ -142,10 +186,14 @@ static int merge_pair(const Elem* a, uint32_t na, const Elem* b, uint32_t nb, El
 // ---------------------------------------------------------------------------
 // the pipeline
 
-// Chunks of a host-buffer sort: 8 from 2^25 elements up, else 1 (one copy in,
-// one sort, one copy out). LSB_HOST_CHUNKS (1, 2, 4, 8 or 16) overrides.
+// Chunks of a host-buffer sort: 16 from 2^28 elements up, 8 from 2^25, else
+// 1 (one copy in, one sort, one copy out). LSB_HOST_CHUNKS (1, 2, 4, 8 or 16)
+// overrides. On one GB300 at 2^30 the call takes 229 ms unchunked, 190.8 /
+// 183.3 / 181.6 ms with 4 / 8 / 16 chunks; the two link copies alone take
+// 170 ms, and with more chunks the merges (one more level each) outgrow the
+// time the copy-in leaves for them.
 int host_chunks(int64_t n) {
-  int c = n >= ((int64_t)1 << 25) ? 8 : 1;
+  int c = n >= ((int64_t)1 << 28) ? 16 : n >= ((int64_t)1 << 25) ? 8 : 1;
   if (const char* e = std::getenv("LSB_HOST_CHUNKS")) {
     const int v = std::atoi(e);
     if (v == 1 || v == 2 || v == 4 || v == 8 || v == 16) c = v;
