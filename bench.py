@@ -13,11 +13,14 @@ itself sweeps L2.
 Prints ONE JSON line (rank 0):
   value        M elements/s, whole job, inputs resident in HBM, CUDA events
   e2e          same metric through the host-buffer C-ABI call
-               (lsb_sort_pairs_host: H2D copy + sort + D2H copy per step)
+               (lsb_sort_pairs_host: every step copies the 16 GiB in and out;
+               chunk copies overlap chunk sorts, the sorted chunks are merged
+               and copied back slice by slice), beside copy_only_ms, the two
+               copies alone
   roofline     dominant kernel: algorithmic bytes per launch / mean launch time,
                against the measured HBM copy bandwidth (MEASURED_PEAKS.json)
   cpu_baseline the oracle's port of the reference algorithm on the host cores
-               (bounded sample), rank 0 at N=1 only
+               (bounded sample; one_rank: the same on one core), rank 0 at N=1 only
   clocks       SM clock samples taken during the timed region
   segmented    4096 arrays of floor(2^U(10,22)) elements: one batched,
                graph-captured sort against a loop of lsb_sort_pairs
@@ -60,7 +63,7 @@ def algorithmic_bytes_per_element(digit_bits: int, passes_run: int) -> int:
 def args_parse(argv=None):
     p = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--steps", type=int, default=20)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", choices=["native", "reference"], default="native")
     p.add_argument("--n", type=int, default=1 << 30)
@@ -203,14 +206,14 @@ def committed_traffic(kernel: str, n: int, digit_bits: int):
 # ---------------------------------------------------------------------------
 # the CPU arm and the cpu_baseline leg
 
-def cpu_sort_rate(sample: int, reps: int, warmup: int = 0, budget_s: float = 30.0):
-    """Times the oracle's port of the reference algorithm (all host cores, one
-    simulated MPI rank per thread) on `sample` uniform elements. Returns
-    (M elem/s over the timed reps, per-rep seconds, threads)."""
+def cpu_sort_rate(sample: int, reps: int, warmup: int = 0, budget_s: float = 30.0, threads: int = 0):
+    """Times the oracle's port of the reference algorithm (one simulated MPI
+    rank per thread; all host cores unless `threads` is given) on `sample`
+    uniform elements. Returns (M elem/s over the timed reps, per-rep seconds, threads)."""
     import oracle
 
     oracle.build(with_ref=False) if not os.path.exists(oracle.ORACLE_SO) else None
-    threads = os.cpu_count() or 1
+    threads = threads or os.cpu_count() or 1
     a = oracle.generate(sample, oracle.DIST_UNIFORM, 0)
     times = []
     for i in range(warmup + reps):
@@ -441,9 +444,13 @@ def gpu_arm(args, ranks: Ranks):
 
     if ranks.rank == 0 and ranks.world == 1 and not args.no_cpu:
         val, times, threads = cpu_sort_rate(args.cpu_sample, 3, warmup=1, budget_s=30.0)
+        one = args.cpu_sample // 4
+        val1, times1, _ = cpu_sort_rate(one, 1, warmup=0, budget_s=30.0, threads=1)
         out["cpu_baseline"] = {"value": round(val, 3), "unit": UNIT, "cores": threads, "kind": "port",
                                "sample": f"{args.cpu_sample} uniform elements, 16-bit digits, "
-                                         f"{len(times)} timed sorts, {threads} simulated ranks"}
+                                         f"{len(times)} timed sorts, {threads} simulated ranks",
+                               "one_rank": {"value": round(val1, 3), "unit": UNIT, "cores": 1,
+                                            "sample": f"{one} uniform elements, 16-bit digits, one rank"}}
     return out
 
 
