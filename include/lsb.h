@@ -134,7 +134,11 @@ int lsb_query(const void* d_workspace, void* stream, lsb_stats_t* stats);
  * buffers are allocated and freed inside the call. This is the call a host
  * program that keeps its arrays in host memory, like the reference
  * (DistributedArray::localPart, mpi/mpi_lsbsort.cpp:105), makes. If h_a is
- * page-locked the copies run at full link speed. */
+ * page-locked the copies run at full link speed. From 2^25 elements the copy
+ * in goes chunk by chunk on a second stream, each chunk is sorted as soon as
+ * it has arrived, the sorted chunks are merged stably, and the result goes
+ * back slice by slice while later slices merge; the output bytes are those of
+ * a single sort. `stream` orders the call after the caller's earlier work on it. */
 int lsb_sort_pairs_host(lsb_elem_t* h_a, int64_t n, int digit_bits, void* stream);
 
 /* Harness: fills d_out[0..n) with the seeded input of distribution `dist`;
