@@ -161,12 +161,14 @@ def test_host_buffer_entry_point(lsb, cuda, oracle):
 def test_host_buffer_pipeline(lsb, cuda, oracle, monkeypatch, chunks):
     """The chunked host-buffer sort (copies overlapped with chunk sorts, then
     stable merges) equals the stable sort: empty and one-element chunks, ties
-    across chunk boundaries (equal keys, Zipf), several output slices."""
+    across chunk and slice boundaries (equal keys, Zipf), one to four output
+    slices."""
     monkeypatch.setenv("LSB_HOST_CHUNKS", str(chunks))
     for n, dist, bits in ((5, oracle.DIST_UNIFORM, 16), (17, oracle.DIST_EQUAL, 8),
                           (300007, oracle.DIST_ZIPF, 16), (300007, oracle.DIST_EQUAL, 11),
                           ((1 << 21) + 3, oracle.DIST_UNIFORM, 8), ((1 << 21) + 3, oracle.DIST_ZIPF, 13),
-                          ((1 << 21) + 3, oracle.DIST_NEARLY_SORTED, 16)):
+                          ((1 << 21) + 3, oracle.DIST_NEARLY_SORTED, 16), ((1 << 22) + 5, oracle.DIST_EQUAL, 16),
+                          ((1 << 22) + 5, oracle.DIST_LOW32, 8)):
         a = oracle.generate(n, dist, 21)
         h = a.copy()
         lsb.sort_pairs_host(h, bits)
