@@ -188,6 +188,20 @@ def test_host_buffer_pipeline_default_size(lsb, cuda, oracle, monkeypatch):
     assert np.array_equal(t.numpy().view(np.uint64), oracle.stable_sort_by_key(a))
 
 
+@pytest.mark.parametrize("variant", [1, 2, 3])
+def test_other_kernel_shapes(lsb, cuda, oracle, monkeypatch, variant):
+    """The selectable CTA shapes of the scatter kernel (LSB_ONESWEEP_VARIANT:
+    the bulk-copy-load kernels 1 and 3, the two-CTA register kernel 2) sort
+    like the default one."""
+    monkeypatch.setenv("LSB_ONESWEEP_VARIANT", str(variant))
+    for bits in (8, 16, 11, 4):
+        for dist, n in ((oracle.DIST_UNIFORM, 300007), (oracle.DIST_ZIPF, 100003), (oracle.DIST_EQUAL, 4097),
+                        (oracle.DIST_NEARLY_SORTED, 65537)):
+            a = oracle.generate(n, dist, 31)
+            assert np.array_equal(_sort(lsb, cuda, a, bits, workspace=True), oracle.stable_sort_by_key(a)), \
+                (variant, bits, dist, n)
+
+
 def test_cpp_driver_runs_and_verifies(lsb, cuda):
     import subprocess
 
