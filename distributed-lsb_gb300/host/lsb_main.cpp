@@ -7,7 +7,8 @@
 // --dist NAME (uniform, low32, zipf, equal, nearly_sorted), --seed S,
 // --warmup W (untimed sorts of a copy of the input before the timed one),
 // --per-pass (sort by a loop of globalShuffle over the digits, the structure
-// of the reference's mySort, instead of one lsb_sort_pairs call).
+// of the reference's mySort, instead of one lsb_sort_pairs call), --help.
+// Other arguments are ignored, as the reference's parser ignores them.
 //
 // Input: key from the seeded splitmix64 stream, value = global index, like
 // the reference's pcg64(rank) generator with val = global index (:686-692).
@@ -44,6 +45,14 @@ static std::ostream& operator<<(std::ostream& os, const SortElement& x) {
   return os << "," << x.val << ")";
 }
 
+static const char* kUsage =
+    "usage: lsb_sort [--n N] [--print] [--verify | --no-verify] [--digit-bits B]\n"
+    "                [--dist uniform|low32|zipf|equal|nearly_sorted] [--seed S] [--warmup W]\n"
+    "                [--per-pass]\n"
+    "Sorts N 16-byte (key, value) elements on the GPU (default N = 100000000, B = 16) and\n"
+    "prints the time like mpi_lsbsort; --verify compares with std::stable_sort by key\n"
+    "(default when N < 128 Mi).\n";
+
 static void print_some(const DeviceArray<SortElement>& A, int64_t k) {
   std::vector<SortElement> h;
   A.copyToHost(h);
@@ -70,7 +79,10 @@ int main(int argc, char** argv) {
       }
       return argv[++i];
     };
-    if (a == "--n") n = std::stoll(next());
+    if (a == "--help" || a == "-h") {
+      std::cout << kUsage;
+      return 0;
+    } else if (a == "--n") n = std::stoll(next());
     else if (a == "--print") printSome = true;
     else if (a == "--verify") verifyLocally = verifySet = true;
     else if (a == "--no-verify") { verifyLocally = false; verifySet = true; }

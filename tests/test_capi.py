@@ -74,3 +74,20 @@ def test_no_device_reports_status(lsb):
     assert lsb.load().lsb_workspace_bytes(1000, 16, ctypes.byref(out)) == lsb.LSB_ERR_NO_DEVICE
     with pytest.raises(lsb.LsbError):
         lsb.workspace_bytes(1000, 16)
+
+
+def test_driver_command_line_without_gpu(lsb):
+    """lsb_sort, the counterpart of the reference's main: --help lists the flags
+    and exits 0; a bad --dist value is refused before any GPU work."""
+    import subprocess
+
+    from lsb_gb300 import _build
+
+    r = subprocess.run([_build.DRIVER_PATH, "--help"], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 0
+    for flag in ("--n", "--print", "--verify", "--no-verify", "--digit-bits", "--dist", "--per-pass"):
+        assert flag in r.stdout, flag
+    r = subprocess.run([_build.DRIVER_PATH, "--dist", "bogus"], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 2 and "unknown --dist" in r.stderr
+    r = subprocess.run([_build.DRIVER_PATH, "--n"], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 2 and "missing value" in r.stderr
