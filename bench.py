@@ -69,7 +69,7 @@ def args_parse(argv=None):
     p.add_argument("--n", type=int, default=1 << 30)
     p.add_argument("--digit-bits", type=int, default=16)
     p.add_argument("--dist", choices=sorted(DIST_NAMES), default="uniform")
-    p.add_argument("--e2e-steps", type=int, default=3)
+    p.add_argument("--e2e-steps", type=int, default=10)
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
     p.add_argument("--no-extra", action="store_true", help="skip the 8-bit-digit side measurement")
@@ -324,8 +324,8 @@ def gpu_arm(args, ranks: Ranks):
     dom = max(prof.items(), key=lambda kv: kv[1][1])[0]
     dom_ms = prof[dom][1] / prof[dom][0]
     # algorithmic bytes per launch of the dominant kernel (per element, x n)
-    per_elem = {"task_scatter": 32, "onesweep_scatter": 32, "task_count": 8, "hist_digits": 8,
-                "final_copy": 32}.get(dom, 0)
+    per_elem = {"task_scatter": 32, "onesweep_scatter": 32, "wide_pass": 32, "task_count": 8,
+                "hist_digits": 8, "hist16": 8, "final_copy": 32}.get(dom, 0)
     peaks = measured_peaks()
     achieved = per_elem * n / (dom_ms / 1e3) / 1e9
     traffic, traffic_src = committed_traffic(dom, n, bits)
@@ -415,9 +415,13 @@ def gpu_arm(args, ranks: Ranks):
             if i >= 1:
                 times.append(dt)
         te = ranks.max(sum(times))
-        ok = bool((h[1:, 0].cpu() >= h[:-1, 0].cpu()).all().item()) if n < (1 << 27) else None
+        # full O(n) check of the last step's output on the device: keys in order,
+        # equal keys in input order, every input index once with its key (the
+        # reference's std::stable_sort comparison, mpi/mpi_lsbsort.cpp:755-784)
+        dev = h.cuda()
+        e2e_bad = lsb.verify(inp, dev)
+        ok = e2e_bad == 0
         # the same bytes copied in and out with nothing in between: the link's floor for this call
-        dev = torch.empty_like(inp)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         dev.copy_(h, non_blocking=True)
@@ -428,10 +432,12 @@ def gpu_arm(args, ranks: Ranks):
         out["e2e"] = {"value": round(n * ranks.world * len(times) / te / 1e6, 3), "unit": UNIT,
                       "h2d_bytes_per_step": 16 * n, "d2h_bytes_per_step": 16 * n,
                       "steps": len(times), "ms_per_step": round(te * 1e3 / len(times), 3),
+                      "p50_ms": round(statistics.median(times) * 1e3, 3),
+                      "p99_ms": round(sorted(times)[min(len(times) - 1, int(0.99 * len(times)))] * 1e3, 3),
                       "copy_only_ms": round(floor_ms, 3),
                       "call": "lsb_sort_pairs_host (pinned host buffer): chunk copies overlapped with "
                               "chunk sorts, stable merges, merged slices copied out while the next merges",
-                      "sorted_check": ok}
+                      "sorted_check": ok, "verify_violations": int(e2e_bad)}
         del h
 
     if not args.no_segmented:

@@ -89,13 +89,18 @@ int pool_alloc(void** ptr, size_t bytes, cudaStream_t st) {
 // ---------------------------------------------------------------------------
 // workspace layout
 
-// How wide digits (12, 14, 16 bits) run inside lsb_sort_pairs: "split"
-// (default) executes each pass as two stable half-width onesweep sub-passes,
-// "task" as one pass of the task family. Read from LSB_WIDE_DIGITS.
-static bool wide_digits_split() {
+// How wide digits run (LSB_WIDE_DIGITS). 16-bit digits: "wide" (default) is
+// one pass per digit through the wide family; "split" runs each 16-bit digit
+// as two stable 8-bit onesweep sub-passes; "task" as one pass of the task
+// family. 12- and 14-bit digits: split (default) or task.
+enum class WideMode { kWide, kSplit, kTask };
+static WideMode wide_mode() {
   const char* e = std::getenv("LSB_WIDE_DIGITS");
-  return !(e && std::strcmp(e, "task") == 0);
+  if (e && std::strcmp(e, "task") == 0) return WideMode::kTask;
+  if (e && std::strcmp(e, "split") == 0) return WideMode::kSplit;
+  return WideMode::kWide;
 }
+static bool wide_digits_split() { return wide_mode() != WideMode::kTask; }
 
 // Look-back ring slots for `tiles` tiles of 2^bits status words: one slot per
 // tile while that costs at most an eighth of the array's bytes (or 64 MiB),
@@ -115,7 +120,24 @@ int plan_layout(int64_t n, int bits, int num_digits, Layout* L, bool allow_split
   *L = Layout();
   L->api_bits = bits;
   L->sub = 1;
-  if (bits > 11 && allow_split && bits % 2 == 0 && bits <= 16 && wide_digits_split()) {
+  if (bits == 16 && !compact && wide_mode() == WideMode::kWide) {
+    // one pass per 16-bit digit (lsb_wide.cu)
+    L->family = Family::kWide;
+    L->bits = 16;
+    L->num_digits = num_digits;
+    L->n = (uint32_t)n;
+    size_t off = kCtrlBytes;
+    L->off_hist = off;
+    off = align_up(off + (size_t)num_digits * 65536u * 4u, 256);
+    L->off_gstart = off;
+    off = align_up(off + (size_t)num_digits * 65536u * 4u, 256);
+    L->off_wide = off;
+    size_t zero_bytes = 0, ring_bytes = 0, offs[9];
+    off = align_up(off + wide_layout_bytes(L->n, &zero_bytes, &ring_bytes, offs), 256);
+    L->total = off;
+    return 0;
+  }
+  if (bits > 11 && (allow_split || compact) && bits % 2 == 0 && bits <= 16 && wide_digits_split()) {
     // a stable sort by digit d equals a stable sort by its low half, then by
     // its high half: half-width digits 2d and 2d+1
     const int half = bits / 2;
@@ -163,6 +185,7 @@ int run_passes(Elem* X, Elem* Y, int first_digit, int target_parity, void* ws, c
   if (cudaMemsetAsync(w, 0, kCtrlBytes, st) != cudaSuccess) return LSB_ERR_CUDA;
   first_digit *= L.sub;  // split wide digits: sub-digits 2d and 2d+1
   int rc = (L.family == Family::kOnesweep) ? onesweep_run(X, Y, first_digit, target_parity, w, L, st)
+           : (L.family == Family::kWide)    ? wide_run(X, Y, first_digit, target_parity, w, L, st)
                                             : task_run(X, Y, first_digit, target_parity, w, L, st);
   if (rc) return rc == 1 ? LSB_ERR_INVALID_ARG : LSB_ERR_CUDA;
   return LSB_OK;
@@ -444,6 +467,19 @@ int lsb_histogram(const lsb_elem_t* d_data, int64_t n, int digit_bits, int64_t* 
     cudaFreeAsync(tmp, st);
     return rc;
   }
+  if (digit_bits == 16) {
+    // byte-packed counters: one read of the keys per three digits
+    void* tmp = nullptr;
+    const uint32_t cnt = (uint32_t)P * nbins;
+    if (int rc = pool_alloc(&tmp, (size_t)cnt * 4u, st)) return rc;
+    int rc = hist16(data, (uint32_t)n, 0, P, (uint32_t*)tmp, st) ? LSB_ERR_CUDA : LSB_OK;
+    if (rc == LSB_OK) {
+      k_u32_to_i64<<<(cnt + 255) / 256, 256, 0, st>>>((uint32_t*)tmp, d_counts, cnt);
+      if (cudaPeekAtLastError() != cudaSuccess) rc = LSB_ERR_CUDA;
+    }
+    cudaFreeAsync(tmp, st);
+    return rc;
+  }
   const uint32_t tasks = task_count(dev, (uint32_t)n);
   void* table = nullptr;
   if (int rc = pool_alloc(&table, (size_t)tasks * nbins * 4u, st)) return rc;
@@ -580,22 +616,37 @@ int lsb_profile_enable(int on) {
   return LSB_OK;
 }
 
-int lsb_selftest_wait_timeout(void* stream, int* device_status) {
-  if (!device_status) return LSB_ERR_INVALID_ARG;
+int lsb_selftest_wait(int which, void* stream, int* device_status) {
+  if (!device_status || which < LSB_WAIT_LOOKBACK || which > LSB_WAIT_SCHEDULER)
+    return LSB_ERR_INVALID_ARG;
   cudaStream_t st = (cudaStream_t)stream;
-  const size_t bytes = kCtrlBytes + 32u;
+  const bool wide = which >= LSB_WAIT_BUCKET_PREFIX;
+  const size_t bytes = wide ? lsb::selftest_wide_bytes() : kCtrlBytes + 32u;
   void* ws = nullptr;
   if (int rc = pool_alloc(&ws, bytes, st)) return rc;
+  unsigned char* w = static_cast<unsigned char*>(ws);
   int rc = LSB_OK;
   Ctrl c{};
-  if (cudaMemsetAsync(ws, 0, bytes, st) != cudaSuccess ||
-      lsb::selftest_lookback_timeout(static_cast<unsigned char*>(ws), st) != 0 ||
-      cudaMemcpyAsync(&c, ws, sizeof c, cudaMemcpyDeviceToHost, st) != cudaSuccess)
-    rc = LSB_ERR_CUDA;
+  if (cudaMemsetAsync(ws, 0, bytes, st) != cudaSuccess) rc = LSB_ERR_CUDA;
+  if (rc == LSB_OK) {
+    int r = 0;
+    switch (which) {
+      case LSB_WAIT_LOOKBACK: r = lsb::selftest_lookback_timeout(w, st); break;
+      case LSB_WAIT_RING_SLOT: r = lsb::selftest_ring_slot(w, st); break;
+      case LSB_WAIT_BULK_COPY: r = lsb::selftest_bulk_copy(w, st); break;
+      default: r = lsb::selftest_wide_wait(which - LSB_WAIT_BUCKET_PREFIX, w, st); break;
+    }
+    if (r != 0 || cudaMemcpyAsync(&c, ws, sizeof c, cudaMemcpyDeviceToHost, st) != cudaSuccess)
+      rc = LSB_ERR_CUDA;
+  }
   cudaFreeAsync(ws, st);
   if (cudaStreamSynchronize(st) != cudaSuccess && rc == LSB_OK) rc = LSB_ERR_CUDA;
   if (rc == LSB_OK) *device_status = (int)c.error;
   return rc;
+}
+
+int lsb_selftest_wait_timeout(void* stream, int* device_status) {
+  return lsb_selftest_wait(LSB_WAIT_LOOKBACK, stream, device_status);
 }
 
 int lsb_profile_read(lsb_kernel_time_t* out, int capacity, int* count) {

@@ -27,6 +27,7 @@ constexpr uint32_t kStatusInconsistent = 1;
 constexpr uint32_t kWhereLookback = 1;
 constexpr uint32_t kWhereRingReuse = 2;
 constexpr uint32_t kWhereScatter = 3;
+constexpr uint32_t kWhereBulkCopy = 6;   // a bulk copy's completion barrier
 
 // Spin limit for every device-side wait: after this many polls (with a
 // nanosleep back-off of up to 256 ns each) the kernel records
@@ -53,6 +54,13 @@ struct Ctrl {
 };
 static_assert(sizeof(Ctrl) <= 1024, "control block must fit its 1 KiB slot");
 constexpr size_t kCtrlBytes = 1024;
+
+// Pass p of the current call was planned away: its digit is the same for
+// every element, and a stable sort by a constant digit is the identity.
+__device__ __forceinline__ bool pass_skipped(const Ctrl* ctrl, int pass) {
+  const uint32_t m = pass < 32 ? ctrl->skip_mask_lo : ctrl->skip_mask_hi;
+  return (m >> (pass & 31)) & 1u;
+}
 
 // A batch of independent arrays sorted together (null tile_seg: one array).
 struct SegDesc {
@@ -184,6 +192,26 @@ __device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t phase) {
       : "memory");
   return ok != 0;
 }
+// Bounded wait until the completion tag at `word` reaches `want` (ring-slot
+// reuse: the readers of a look-back slot report done). `got` is a value of
+// the word already read. Returns true, after recording kStatusTimeout with
+// kWhereRingReuse, if the tag stays below `want` for kSpinLimit polls (or an
+// error is raised elsewhere meanwhile).
+__device__ __forceinline__ bool wait_done_tag(const uint32_t* word, uint32_t want, uint32_t got,
+                                              bool acquire, Ctrl* ctrl) {
+  uint32_t ns = 8, it = 0;
+  while (got < want) {
+    if (++it >= kSpinLimit || ((it & 63u) == 0u && error_raised(ctrl))) {
+      record_error(ctrl, kStatusTimeout, kWhereRingReuse);
+      return true;
+    }
+    __nanosleep(ns);
+    if (ns < 256) ns <<= 1;
+    got = acquire ? ld_acquire_u32(word) : ld_relaxed_u32(word);
+  }
+  return false;
+}
+
 // Bounded wait for phase `phase` of the barrier: false after kSpinLimit tries.
 __device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t phase) {
   for (uint32_t it = 0; it < kSpinLimit; it++)

@@ -5,6 +5,10 @@
 //  * "onesweep" family (digit_bits <= 11): one upfront read of the keys builds
 //    the counts of every digit, then one stable scatter kernel per pass whose
 //    tiles resolve their global offsets by decoupled look-back.
+//  * "wide" family (digit_bits 16, the reference's RADIX): one pass per
+//    16-bit digit and one HBM round trip per pass; tiles are sorted by the
+//    digit's high byte into an L2-resident chunk buffer, then each high-byte
+//    bucket of a chunk is gathered and placed by its low byte (lsb_wide.cu).
 //  * "task" family (digit_bits >= 12, the reference's 16-bit digits): per pass
 //    a count kernel over contiguous tasks, a digit-major scan of the
 //    [digit][task] count table and a stable scatter -- the reference's own
@@ -28,7 +32,7 @@ struct DeviceInfo {
 // Properties of the current device (cached per device id).
 int current_device_info(DeviceInfo* info);
 
-enum class Family { kOnesweep = 0, kTask = 1 };
+enum class Family { kOnesweep = 0, kTask = 1, kWide = 2 };
 
 // Byte offsets inside the caller's workspace (all 256-byte aligned).
 struct Layout {
@@ -52,6 +56,10 @@ struct Layout {
   size_t off_totals = 0;  // uint32 [2^b]         digit totals
   size_t off_dstart = 0;  // uint32 [2^b]         exclusive digit starts
   uint32_t tasks = 0;
+  // wide family: hist and gstart above ([num_digits][65536]) plus the pass
+  // region of lsb_wide.cu (scheduler, bucket sizes, running prefixes, chunk
+  // buffers, piece tables, status ring)
+  size_t off_wide = 0;
 };
 
 // allow_split: digits of 12, 14 or 16 bits may run as two half-width
@@ -71,10 +79,33 @@ int onesweep_run(Elem* X, Elem* Y, int first_digit, int target_parity, unsigned 
                  const Layout& L, cudaStream_t st);
 int task_run(Elem* X, Elem* Y, int first_digit, int target_parity, unsigned char* ws,
              const Layout& L, cudaStream_t st);
+int wide_run(Elem* X, Elem* Y, int first_digit, int target_parity, unsigned char* ws,
+             const Layout& L, cudaStream_t st);
+// Bytes of the wide family's pass region for n elements; offs[0..8] receive
+// the offsets of its parts, *pass_zero_bytes the size of the leading part
+// that is cleared before every pass and *ring_bytes that of the status ring.
+size_t wide_layout_bytes(uint32_t n, size_t* pass_zero_bytes, size_t* ring_bytes, size_t offs[9]);
+// Counts of the 16-bit digits [first_digit, first_digit + num_digits) into
+// d_counts[num_digits][65536] (uint32), one read of the keys per three digits.
+int hist16(const Elem* data, uint32_t n, int first_digit, int num_digits, uint32_t* d_counts,
+           cudaStream_t st);
+
+// Pass plan for num_digits digits of `bits` bits: exclusive digit starts,
+// constant digits (skipped), buffer parity of every pass (lsb_onesweep.cu).
+__global__ void __launch_bounds__(1024) k_plan(const uint32_t* __restrict__ ghist, uint32_t* __restrict__ gstart, uint32_t n,
+                       int bits, int num_digits, int target_parity, int api_bits, int sub, Ctrl* ctrl);
 uint32_t onesweep_tile_elems(int bits);
 // the look-back wait of the sort kernels on a predecessor that never publishes
 // (failure-detection self-test); ws: kCtrlBytes + 32 bytes, zeroed by the caller
 int selftest_lookback_timeout(unsigned char* ws, cudaStream_t st);
+// the same for the ring-slot reuse wait and a bulk copy's completion barrier
+// (ws: kCtrlBytes + 32 bytes, zeroed), and for the 16-bit pass's waits
+// (which: 0 bucket prefix, 1 bucket look-back, 2 scheduler; ws:
+// selftest_wide_bytes(), zeroed)
+int selftest_ring_slot(unsigned char* ws, cudaStream_t st);
+int selftest_bulk_copy(unsigned char* ws, cudaStream_t st);
+size_t selftest_wide_bytes();
+int selftest_wide_wait(int which, unsigned char* ws, cudaStream_t st);
 // explicit kernel shape (variant 0: 512 threads x 16, 1 CTA/SM; 2: 256 x 16, 2 CTAs/SM)
 uint32_t onesweep_tile_elems_v(int bits, int variant);
 uint32_t onesweep_grid_v(int bits, int variant, const DeviceInfo& dev, uint32_t tiles);

@@ -10,8 +10,10 @@
 // caller still passes the two element arrays.
 //
 // Limits: digit widths 1..8 (the onesweep kernels, whose scratch does not grow
-// with n) and the scratch of kNoallocScratchBytes below; a call that would
-// need more is rejected before any GPU work.
+// with n), and 12, 14 and 16 (the reference's width), each digit run as two
+// stable sub-passes of half its width; the scratch of kNoallocScratchBytes
+// below. Other widths are rejected with LSB_ERR_INVALID_ARG before any GPU
+// work.
 #include <mutex>
 #include <vector>
 
@@ -40,10 +42,14 @@ static int noalloc_scratch(void** out) {
   std::lock_guard<std::mutex> lk(g_noalloc_mu);
   if ((int)g_noalloc_addr.size() <= dev) g_noalloc_addr.resize(dev + 1, nullptr);
   if (!g_noalloc_addr[dev]) {
+    // With lazy module loading (the CUDA default) this first lookup also loads
+    // the module and reserves the array; if the device's memory is already
+    // taken, that fails with cudaErrorMemoryAllocation.
     void* p = nullptr;
-    if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) {
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p) {
       cudaGetLastError();
-      return LSB_ERR_CUDA;
+      return e == cudaErrorMemoryAllocation ? LSB_ERR_NO_MEMORY : LSB_ERR_CUDA;
     }
     g_noalloc_addr[dev] = p;
   }
@@ -56,8 +62,10 @@ static int noalloc_scratch(void** out) {
 extern "C" int lsb_sort_pairs_noalloc(lsb_elem_t* d_a, lsb_elem_t* d_b, int64_t n, int digit_bits,
                                       void* stream) {
   using namespace lsb;
-  if (digit_bits < 1 || n < 0) return LSB_ERR_INVALID_ARG;
-  if (digit_bits > 8 || n > LSB_MAX_ELEMENTS) return LSB_ERR_TOO_LARGE;
+  const bool width_ok = (digit_bits >= 1 && digit_bits <= 8) || digit_bits == 12 || digit_bits == 14 ||
+                        digit_bits == 16;
+  if (!width_ok || n < 0) return LSB_ERR_INVALID_ARG;
+  if (n > LSB_MAX_ELEMENTS) return LSB_ERR_TOO_LARGE;
   if (n > 0 && (!d_a || !d_b)) return LSB_ERR_INVALID_ARG;
   if (n > 0 && ((((uintptr_t)d_a) | ((uintptr_t)d_b)) & 15u)) return LSB_ERR_ALIGNMENT;
   const uintptr_t a = (uintptr_t)d_a, b = (uintptr_t)d_b, len = (uintptr_t)n * 16u;

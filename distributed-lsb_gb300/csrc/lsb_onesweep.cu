@@ -174,11 +174,6 @@ __global__ void __launch_bounds__(kPlanThreads)
   }
 }
 
-__device__ __forceinline__ bool pass_skipped(const Ctrl* ctrl, int pass) {
-  const uint32_t m = pass < 32 ? ctrl->skip_mask_lo : ctrl->skip_mask_hi;
-  return (m >> (pass & 31)) & 1u;
-}
-
 // ---------------------------------------------------------------------------
 // the onesweep scatter
 
@@ -517,20 +512,11 @@ __global__ void __launch_bounds__(THREADS, MINB)
       for (uint32_t j = 1u + threadIdx.x; j <= gridDim.x; j += THREADS) {
         const uint32_t y = x + j;
         if (y >= t) break;
-        const uint32_t want = ring_tag(pass, y);
-        uint32_t got = (j == 1u + threadIdx.x) ? done_tag : ld_relaxed_u32(done + y % ring_tiles);
-        uint32_t ns = 8, it = 0;
-        while (got < want) {
-          if (++it >= kSpinLimit || ((it & 63u) == 0u && error_raised(ctrl))) {
-            record_error(ctrl, kStatusTimeout, kWhereRingReuse);
-            timed_out = true;
-            break;
-          }
-          __nanosleep(ns);
-          if (ns < 256) ns <<= 1;
-          got = ld_relaxed_u32(done + y % ring_tiles);
+        const uint32_t got = (j == 1u + threadIdx.x) ? done_tag : ld_relaxed_u32(done + y % ring_tiles);
+        if (wait_done_tag(done + y % ring_tiles, ring_tag(pass, y), got, false, ctrl)) {
+          timed_out = true;
+          break;
         }
-        if (timed_out) break;
       }
       // acquire: the readers' done releases happen before this tile's writes
       // to the slot (the fence follows the relaxed reads that observed them)
@@ -775,7 +761,7 @@ __global__ void __launch_bounds__(THREADS, 1)
     //    item k of lane l in warp w is element w*32*K + k*32 + l)
     const bool arrived = mbar_wait_bounded(bar, phase);
     if (__syncthreads_or(!arrived)) {
-      record_error(ctrl, kStatusTimeout, kWhereLookback);
+      record_error(ctrl, kStatusTimeout, kWhereBulkCopy);
       break;
     }
     copy_pending = false;
@@ -829,18 +815,11 @@ __global__ void __launch_bounds__(THREADS, 1)
       for (uint32_t j = 1 + threadIdx.x; j <= gridDim.x; j += THREADS) {
         const uint32_t y = x + j;
         if (y >= t) break;
-        const uint32_t want = ring_tag(pass, y);
-        uint32_t ns = 8, it = 0;
-        while (ld_acquire_u32(done + (y % ring_tiles)) < want) {
-          if (++it >= kSpinLimit || ((it & 63u) == 0u && error_raised(ctrl))) {
-            record_error(ctrl, kStatusTimeout, kWhereRingReuse);
-            timed_out = true;
-            break;
-          }
-          __nanosleep(ns);
-          if (ns < 256) ns <<= 1;
+        const uint32_t* word = done + (y % ring_tiles);
+        if (wait_done_tag(word, ring_tag(pass, y), ld_acquire_u32(word), true, ctrl)) {
+          timed_out = true;
+          break;
         }
-        if (timed_out) break;
       }
       __syncthreads();
     }
@@ -1036,6 +1015,36 @@ __global__ void k_selftest_lookback(Ctrl* ctrl, uint64_t* ring) {
   // never finds a published predecessor
   (void)walk_one(ring, 2u, 1u, 0u, 0, 1u, ctrl, &timed_out, &steps, &polls);
   ctrl->lookback_polls = polls;
+}
+
+// the ring-slot reuse wait: a reader of the slot (tile 1 of pass 0) never
+// reports done, so its completion tag stays zero
+__global__ void k_selftest_ring_slot(Ctrl* ctrl, uint32_t* done) {
+  if (threadIdx.x != 0) return;
+  (void)wait_done_tag(done, ring_tag(0, 1u), ld_relaxed_u32(done), false, ctrl);
+}
+
+// a bulk copy's completion barrier: 16 bytes are expected that no copy
+// delivers, so the barrier's phase never completes
+__global__ void k_selftest_bulk_copy(Ctrl* ctrl) {
+  __shared__ __align__(8) uint64_t s_bar;
+  if (threadIdx.x != 0) return;
+  const uint32_t bar = smem_u32(&s_bar);
+  mbar_init(bar, 1);
+  fence_mbar_init();
+  mbar_arrive_expect_tx(bar, 16u);
+  if (!mbar_wait_bounded(bar, 0u)) record_error(ctrl, kStatusTimeout, kWhereBulkCopy);
+}
+
+int selftest_ring_slot(unsigned char* ws, cudaStream_t st) {
+  Ctrl* ctrl = reinterpret_cast<Ctrl*>(ws);
+  k_selftest_ring_slot<<<1, 32, 0, st>>>(ctrl, reinterpret_cast<uint32_t*>(ws + kCtrlBytes));
+  return cudaPeekAtLastError() == cudaSuccess ? 0 : 5;
+}
+
+int selftest_bulk_copy(unsigned char* ws, cudaStream_t st) {
+  k_selftest_bulk_copy<<<1, 32, 0, st>>>(reinterpret_cast<Ctrl*>(ws));
+  return cudaPeekAtLastError() == cudaSuccess ? 0 : 5;
 }
 
 int selftest_lookback_timeout(unsigned char* ws, cudaStream_t st) {

@@ -68,6 +68,7 @@ SIGNATURES = {
     "lsb_profile_enable": (ctypes.c_int, [ctypes.c_int]),
     "lsb_profile_read": (ctypes.c_int, [_P, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]),
     "lsb_selftest_wait_timeout": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int)]),
+    "lsb_selftest_wait": (ctypes.c_int, [ctypes.c_int, _P, ctypes.POINTER(ctypes.c_int)]),
 }
 
 
@@ -382,6 +383,21 @@ def selftest_wait_timeout(stream=None) -> int:
     st = ctypes.c_int(-1)
     _check(load().lsb_selftest_wait_timeout(_stream_ptr(stream), ctypes.byref(st)),
            "lsb_selftest_wait_timeout")
+    return st.value
+
+
+WAIT_LOOKBACK, WAIT_RING_SLOT, WAIT_BULK_COPY = 0, 1, 2
+WAIT_BUCKET_PREFIX, WAIT_BUCKET_LOOKBACK, WAIT_SCHEDULER = 3, 4, 5
+WAITS = {"lookback": 0, "ring_slot": 1, "bulk_copy": 2, "bucket_prefix": 3, "bucket_lookback": 4,
+         "scheduler": 5}
+
+
+def selftest_wait(which: int, stream=None) -> int:
+    """Runs one bounded device wait of the library's kernels (WAIT_*) on a
+    flag nothing sets; returns the device status it ended with
+    (LSB_ERR_DEVICE_TIMEOUT when the wait ran out as designed)."""
+    st = ctypes.c_int(-1)
+    _check(load().lsb_selftest_wait(which, _stream_ptr(stream), ctypes.byref(st)), "lsb_selftest_wait")
     return st.value
 
 

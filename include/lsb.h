@@ -257,13 +257,19 @@ int lsb_server_destroy(lsb_server_t* server);
  * cannot take the device-wide synchronisation of cudaMalloc/cudaFree, code
  * that must not fail half-way for lack of memory. It sorts d_a like
  * lsb_sort_pairs (d_b scratch, result in d_a, same bytes) but takes its
- * scratch from an 8 MiB array compiled into the library, which every GPU that
- * loads the library holds until the process exits; it calls no allocator.
- * Limits: digit_bits 1..8 (LSB_ERR_TOO_LARGE otherwise) and n up to
- * LSB_MAX_ELEMENTS; if the scratch this GPU's kernel configuration needs is
- * more than 8 MiB the call returns LSB_ERR_WORKSPACE before any GPU work.
- * The first call on each device looks up the array's device address (with
- * that device current); make that first call before any stream capture.
+ * scratch from an 8 MiB array compiled into the library; it calls no
+ * allocator. The array belongs to the library's code module: it is reserved
+ * on a device when that module is loaded there, which with CUDA's default
+ * lazy loading is the first call of this function on the device (that call
+ * also loads the sort kernels), and it is held until the process exits.
+ * So make the first call on each device at start-up, before an arena takes
+ * the device's free memory and before any stream capture on it; a first
+ * call that finds no memory left returns LSB_ERR_NO_MEMORY.
+ * Limits: digit_bits 1..8, 12, 14 or 16 (a 12-, 14- or 16-bit digit runs as
+ * two stable passes of half its width; other widths: LSB_ERR_INVALID_ARG)
+ * and n up to LSB_MAX_ELEMENTS (LSB_ERR_TOO_LARGE); if the scratch this GPU's
+ * kernel configuration needs is more than 8 MiB the call returns
+ * LSB_ERR_WORKSPACE before any GPU work.
  * All calls share the one array and it keeps the last call's contents (each
  * call clears what must start at zero): calls whose GPU work overlaps, on
  * different streams or host threads, race and corrupt each other's results.
@@ -294,6 +300,22 @@ int lsb_profile_read(lsb_kernel_time_t* out, int capacity, int* count);
  * points would return for it (LSB_ERR_DEVICE_TIMEOUT) and the context stays
  * usable. Blocking; allocates a few KiB. */
 int lsb_selftest_wait_timeout(void* stream, int* device_status);
+
+/* The same self-test for each bounded wait of the library's kernels (no
+ * counterpart in the reference). Each runs the wait's own device code on a
+ * flag that nothing ever sets, so the wait runs out (a second or a few),
+ * the kernel records the timeout and returns, and *device_status receives
+ * LSB_ERR_DEVICE_TIMEOUT; the context stays usable. `which`: */
+enum lsb_wait {
+  LSB_WAIT_LOOKBACK = 0,        /* scatter pass: look-back on a predecessor tile that never publishes */
+  LSB_WAIT_RING_SLOT = 1,       /* scatter pass: reuse of a look-back ring slot whose reader never finishes */
+  LSB_WAIT_BULK_COPY = 2,       /* a bulk copy's completion barrier that no copy completes */
+  LSB_WAIT_BUCKET_PREFIX = 3,   /* 16-bit pass: a bucket's running prefix an earlier chunk never hands on */
+  LSB_WAIT_BUCKET_LOOKBACK = 4, /* 16-bit pass: look-back among one bucket's tiles, predecessor silent */
+  LSB_WAIT_SCHEDULER = 5        /* 16-bit pass itself: no runnable work ever appears (a chunk plan
+                                   nobody publishes) */
+};
+int lsb_selftest_wait(int which, void* stream, int* device_status);
 
 #ifdef __cplusplus
 }

@@ -26,7 +26,12 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "_build", "liblsb_oracle.so")
 REF_SO = os.path.join(HERE, "_ref", "liblsb_ref.so")
 REF_MAIN = os.path.join(HERE, "_ref", "mpi_lsbsort")
-REFERENCE_SRC = "/root/reference/mpi/mpi_lsbsort.cpp"
+# The reference checkout: LSB_REFERENCE_DIR when set, otherwise a checkout
+# named `reference` next to this repository (absent on machines that only run
+# the prebuilt checker).
+REFERENCE_DIR = os.environ.get("LSB_REFERENCE_DIR") or os.path.join(
+    os.path.dirname(os.path.dirname(HERE)), "reference")
+REFERENCE_SRC = os.path.join(REFERENCE_DIR, "mpi", "mpi_lsbsort.cpp")
 
 DIST_UNIFORM, DIST_LOW32, DIST_ZIPF, DIST_EQUAL, DIST_NEARLY_SORTED = 0, 1, 2, 3, 4
 DIST_NAMES = {"uniform": 0, "low32": 1, "zipf": 2, "equal": 3, "nearly_sorted": 4}
@@ -46,7 +51,7 @@ def build(with_ref: bool | None = None) -> None:
     if with_ref is None:
         with_ref = os.path.exists(REFERENCE_SRC)
     if with_ref:
-        subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True)
+        subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={REFERENCE_DIR}"], check=True)
 
 
 def lib():

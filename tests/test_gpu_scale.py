@@ -50,3 +50,19 @@ def test_2p30_uniform(lsb, cuda, bits):
         pytest.skip("needs ~50 GB of free device memory")
     bad, st = _sort_and_check(lsb, cuda, 1 << 30, lsb.DIST_UNIFORM, bits)
     assert bad == 0 and st.passes_run == 64 // bits
+
+
+@pytest.mark.parametrize("dist", [0, 2])
+def test_2p28_host_buffer_default_pipeline(lsb, cuda, dist):
+    """The host-buffer call at its default geometry from 2^28 elements (16
+    chunks sorted as they arrive over the link, stable merges, 16 output
+    slices copied back while the next merge), checked in O(n) on the device."""
+    n = 1 << 28
+    inp = lsb.generate(n, dist, 5)
+    h = inp.cpu().pin_memory()
+    lsb.sort_pairs_host(h, 16)
+    out = h.cuda()
+    del h
+    assert lsb.verify(inp, out) == 0
+    del inp, out
+    cuda.cuda.empty_cache()
