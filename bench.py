@@ -79,6 +79,9 @@ def args_parse(argv=None):
     p.add_argument("--seg-steps", type=int, default=3)
     p.add_argument("--seg-seed", type=int, default=2024)
     p.add_argument("--no-serving", action="store_true", help="skip the request-loop leg")
+    p.add_argument("--no-configs", action="store_true",
+                   help="skip the timed small (2^24) and skew (2^28) configurations")
+    p.add_argument("--config-steps", type=int, default=10)
     p.add_argument("--requests", type=int, default=10000)
     p.add_argument("--rate", type=float, default=400.0, help="Poisson arrival rate, requests/s")
     p.add_argument("--serve-slots", type=int, default=4)
@@ -254,6 +257,50 @@ def cpu_arm(args, ranks: Ranks):
 # ---------------------------------------------------------------------------
 # the GPU arm
 
+def configs_leg(args, lsb, torch, peaks: dict) -> dict:
+    """The other single-array configurations, each timed like the headline
+    (input restored from a resident copy before every step, CUDA events,
+    checked with the O(n) device verifier): the reference's CPU-runnable size
+    2^24, and 2^28 in the four skewed key distributions, with the sort's
+    roofline on the passes it actually ran (8 B + 32 B per executed pass)."""
+    bits = 16
+    cases = [("small_2p24_uniform", 1 << 24, "uniform"),
+             ("skew_2p28_low32", 1 << 28, "low32"), ("skew_2p28_zipf", 1 << 28, "zipf"),
+             ("skew_2p28_equal", 1 << 28, "equal"), ("skew_2p28_nearly_sorted", 1 << 28, "nearly_sorted")]
+    res = {}
+    for name, n, dist in cases:
+        inp = lsb.generate(n, DIST_NAMES[dist], seed=11)
+        A = torch.empty_like(inp)
+        B = torch.empty_like(inp)
+        ws = lsb.alloc_workspace(n, bits)
+        stream = torch.cuda.current_stream()
+        times = []
+        for i in range(3 + args.config_steps):
+            A.copy_(inp)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            lsb.sort_pairs(A, B, bits, workspace=ws)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            if i >= 3:
+                times.append(e0.elapsed_time(e1))
+        st = lsb.query(ws)
+        bad = lsb.verify(inp, A)
+        ms = statistics.mean(times)
+        per_elem = algorithmic_bytes_per_element(bits, st.passes_run)
+        gbs = per_elem * n / (ms / 1e3) / 1e9
+        res[name] = {"n": n, "dist": dist, "digit_bits": bits, "steps": len(times),
+                     "ms_per_sort": round(ms, 4), "p50_ms": round(statistics.median(times), 4),
+                     "value": round(n / (ms / 1e3) / 1e6, 3), "unit": UNIT,
+                     "passes_run": st.passes_run, "skipped_mask": st.skipped_mask,
+                     "final_copy": st.final_copy, "verify_violations": int(bad),
+                     "sort_roofline": {"algorithmic_bytes_per_element": per_elem, "achieved_gbs": round(gbs, 1),
+                                       "frac": round(gbs / peaks["hbm_gbs"], 4)}}
+        del inp, A, B, ws
+        torch.cuda.empty_cache()
+    return res
+
+
 def gpu_arm(args, ranks: Ranks):
     import torch
 
@@ -400,6 +447,9 @@ def gpu_arm(args, ranks: Ranks):
         if bits in (12, 14, 16):
             out["single_pass_task_family"] = time_sorts(bits, reps=2, env={"LSB_WIDE_DIGITS": "task"})
 
+    if not args.no_configs:
+        out["configs"] = configs_leg(args, lsb, torch, peaks)
+
     # e2e through the host-buffer entry point
     if not args.no_e2e:
         del A, B, ws
@@ -462,65 +512,43 @@ def gpu_arm(args, ranks: Ranks):
 
 def segmented_leg(args, lsb, torch, ranks) -> dict:
     """Batched segmented sort: 4096 arrays with sizes floor(2^U(10, 22)) (seeded),
-    uniform keys, value = index; one CUDA-graph launch with the autotuned
-    configuration against a loop of lsb_sort_pairs (16-bit digits) over the
-    same arrays. Both start from the same unsorted input; outputs must match."""
+    uniform keys, value = index. The C++ driver (lsb_sort --segments-file)
+    sorts the batch twice from the same unsorted input: by a C++ loop of
+    lsb_sort_pairs over the arrays (16-bit digits, one workspace sized once for
+    the largest array), and by one launch of the batched call's CUDA graph
+    with the autotuned configuration; the outputs must be byte-identical."""
     import numpy as np
+
+    from lsb_gb300 import _build
 
     rng = np.random.default_rng(args.seg_seed)
     sizes = np.floor(2.0 ** rng.uniform(10, 22, size=args.segments)).astype(np.int64)
     off = np.zeros(len(sizes) + 1, dtype=np.int64)
     off[1:] = np.cumsum(sizes)
     total = int(off[-1])
-    stream = torch.cuda.current_stream()
-    src = lsb.generate(total, 0, seed=1000 + ranks.rank)
-    A = torch.empty_like(src)
-    B = torch.empty_like(src)
-    offs = torch.from_numpy(off).cuda()
-    tuning = lsb.tune_segmented(off)
-    ws = lsb.alloc_segmented_workspace(total, len(sizes), tuning.digit_bits)
-    graph = lsb.SegmentedGraph(A, B, offs, tuning, ws)
-
-    def timed(fn, reps, warm):
-        ms = []
-        for i in range(warm + reps):
-            A.copy_(src)
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
-            fn()
-            e1.record(stream)
-            torch.cuda.synchronize()
-            if i >= warm:
-                ms.append(e0.elapsed_time(e1))
-        return ms
-
-    batched = timed(lambda: graph.launch(), args.seg_steps, 1)
-    batched_out = A.clone()
-    big = int(sizes.max())
-    ws1 = lsb.alloc_workspace(big, 16)
-    views = [(A[off[s]:off[s + 1]], B[off[s]:off[s + 1]]) for s in range(len(sizes)) if sizes[s] > 0]
-
-    def loop():
-        for a_s, b_s in views:
-            lsb.sort_pairs(a_s, b_s, 16, workspace=ws1[: max(256, lsb.workspace_bytes(a_s.shape[0], 16))])
-
-    looped = timed(loop, max(1, args.seg_steps - 1), 1)
-    identical = bool(torch.equal(batched_out, A))
-    graph.close()
-    bms, lms = statistics.mean(batched), statistics.mean(looped)
-    res = {
-        "segments": len(sizes), "elements": total, "size_law": "floor(2^U(10,22))",
-        "tuning": {"digit_bits": tuning.digit_bits, "variant": tuning.variant},
+    fd, path = tempfile.mkstemp(suffix=".offsets")
+    os.close(fd)
+    try:
+        off.astype("<i8").tofile(path)
+        r = subprocess.run([_build.DRIVER_PATH, "--segments-file", path, "--digit-bits", "16",
+                            "--seed", str(1000 + ranks.rank), "--steps", str(args.seg_steps)],
+                           capture_output=True, text=True, timeout=1800)
+    finally:
+        os.unlink(path)
+    if r.returncode != 0:
+        raise RuntimeError(f"lsb_sort --segments-file failed ({r.returncode}): {r.stdout[-2000:]} {r.stderr[-2000:]}")
+    d = json.loads(r.stdout.strip().splitlines()[-1])
+    bms, lms = d["batched_ms"], d["loop_ms"]
+    return {
+        "segments": d["segments"], "elements": total, "size_law": "floor(2^U(10,22))",
+        "tuning": d["tuning"], "steps": d["steps"],
         "batched_ms": round(bms, 3), "loop_ms": round(lms, 3), "speedup": round(lms / bms, 3),
         "batched_value": round(total / (bms / 1e3) / 1e6, 3), "loop_value": round(total / (lms / 1e3) / 1e6, 3),
-        "unit": UNIT, "identical_outputs": identical,
-        "batched_p50_ms": round(statistics.median(batched), 3),
-        "batched_p99_ms": round(sorted(batched)[min(len(batched) - 1, int(0.99 * len(batched)))], 3),
-        "loop_call": "lsb_sort_pairs per array, 16-bit digits, one workspace, Python ctypes loop",
+        "unit": UNIT, "identical_outputs": d["identical_outputs"],
+        "loop_call": "C++ loop of lsb_sort_pairs per array (lsb_sort --segments-file), 16-bit digits, "
+                     "one workspace sized once for the largest array",
+        "batched_call": "lsb_graph_launch of lsb_graph_capture_segmented with lsb_tune_segmented's choice",
     }
-    del A, B, src, ws, ws1, views
-    torch.cuda.empty_cache()
-    return res
 
 
 def serving_leg(args, lsb, torch, ranks) -> dict:

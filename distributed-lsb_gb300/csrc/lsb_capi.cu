@@ -89,16 +89,16 @@ int pool_alloc(void** ptr, size_t bytes, cudaStream_t st) {
 // ---------------------------------------------------------------------------
 // workspace layout
 
-// How wide digits run (LSB_WIDE_DIGITS). 16-bit digits: "wide" (default) is
-// one pass per digit through the wide family; "split" runs each 16-bit digit
-// as two stable 8-bit onesweep sub-passes; "task" as one pass of the task
+// How wide digits run (LSB_WIDE_DIGITS). 16-bit digits: "split" (default)
+// runs each 16-bit digit as two stable 8-bit onesweep sub-passes; "wide" is
+// one pass per digit through the wide family; "task" one pass of the task
 // family. 12- and 14-bit digits: split (default) or task.
 enum class WideMode { kWide, kSplit, kTask };
 static WideMode wide_mode() {
   const char* e = std::getenv("LSB_WIDE_DIGITS");
   if (e && std::strcmp(e, "task") == 0) return WideMode::kTask;
-  if (e && std::strcmp(e, "split") == 0) return WideMode::kSplit;
-  return WideMode::kWide;
+  if (e && std::strcmp(e, "wide") == 0) return WideMode::kWide;
+  return WideMode::kSplit;
 }
 static bool wide_digits_split() { return wide_mode() != WideMode::kTask; }
 
@@ -471,8 +471,16 @@ int lsb_histogram(const lsb_elem_t* d_data, int64_t n, int digit_bits, int64_t* 
     // byte-packed counters: one read of the keys per three digits
     void* tmp = nullptr;
     const uint32_t cnt = (uint32_t)P * nbins;
-    if (int rc = pool_alloc(&tmp, (size_t)cnt * 4u, st)) return rc;
-    int rc = hist16(data, (uint32_t)n, 0, P, (uint32_t*)tmp, st) ? LSB_ERR_CUDA : LSB_OK;
+    if (int rc = pool_alloc(&tmp, (size_t)cnt * 4u + kCtrlBytes, st)) return rc;
+    if (cudaMemsetAsync(static_cast<unsigned char*>(tmp) + (size_t)cnt * 4u, 0, kCtrlBytes, st) != cudaSuccess) {
+      cudaFreeAsync(tmp, st);
+      return LSB_ERR_CUDA;
+    }
+    // the control block of the one-read form sits behind the counts
+    int rc = hist16(data, (uint32_t)n, 0, P, (uint32_t*)tmp, st,
+                    reinterpret_cast<Ctrl*>(static_cast<unsigned char*>(tmp) + (size_t)cnt * 4u))
+                 ? LSB_ERR_CUDA
+                 : LSB_OK;
     if (rc == LSB_OK) {
       k_u32_to_i64<<<(cnt + 255) / 256, 256, 0, st>>>((uint32_t*)tmp, d_counts, cnt);
       if (cudaPeekAtLastError() != cudaSuccess) rc = LSB_ERR_CUDA;

@@ -51,6 +51,9 @@ struct Ctrl {
   uint32_t lookback_polls;         // diagnostics: windows that found a predecessor unpublished
   uint32_t parity[kMaxPasses + 1]; // parity[p]: 0 = pass p reads X, writes Y; 1 = reads Y, writes X
   uint32_t ticket[kMaxPasses];     // tile dispenser per pass (in-order tile dispatch)
+  // diagnostics of the 16-bit pass when LSB_WIDE_PROFILE is set: SM cycles
+  // and counts per phase, summed over CTAs, for its first four passes
+  unsigned long long wide_prof[4][12];
 };
 static_assert(sizeof(Ctrl) <= 1024, "control block must fit its 1 KiB slot");
 constexpr size_t kCtrlBytes = 1024;

@@ -156,7 +156,10 @@ struct SegLayout {
          off_done = 0, total = 0;
 };
 
-static int seg_plan_layout(int64_t n, int64_t nseg, int digit_bits, int variant, SegLayout* L) {
+// ctas: persistent CTAs of the scatter passes (0 = every resident slot: SMs x
+// CTAs per SM); fewer CTAs keep fewer tiles in flight at once.
+static int seg_plan_layout(int64_t n, int64_t nseg, int digit_bits, int variant, SegLayout* L,
+                           int ctas = 0) {
   DeviceInfo dev;
   if (int rc = current_device_info(&dev)) return rc;
   *L = SegLayout();
@@ -177,6 +180,7 @@ static int seg_plan_layout(int64_t n, int64_t nseg, int digit_bits, int variant,
   L->tile = onesweep_tile_elems_v(bits, variant);
   L->max_tiles = (uint32_t)(((uint64_t)n + L->tile - 1) / L->tile + (uint64_t)nseg);
   L->grid = onesweep_grid_v(bits, variant, dev, std::max<uint32_t>(1u, L->max_tiles));
+  if (ctas > 0) L->grid = std::max<uint32_t>(1u, std::min<uint32_t>(L->grid, (uint32_t)ctas));
   L->ring_tiles = ring_slots((uint64_t)n, L->max_tiles, bits, L->grid, false);
   const size_t nbins = (size_t)1 << bits;
   size_t off = kCtrlBytes;
@@ -256,6 +260,7 @@ static int tuning_variant(const lsb_tuning_t* t) {
 static int tuning_bits(const lsb_tuning_t* t) {
   return (t && t->digit_bits >= 1 && t->digit_bits <= 16) ? t->digit_bits : 8;
 }
+static int tuning_ctas(const lsb_tuning_t* t) { return (t && t->ctas > 0) ? t->ctas : 0; }
 
 static int seg_check(const lsb_elem_t* a, const lsb_elem_t* b, int64_t n, const int64_t* off,
                      int64_t nseg) {
@@ -305,7 +310,7 @@ int lsb_sort_segmented(lsb_elem_t* d_a, lsb_elem_t* d_b, int64_t n_total,
   if (n_total <= 1 || nseg == 0) return LSB_OK;
   SegLayout L;
   if (int rc = seg_plan_layout(n_total, nseg, tuning_bits(opt_tuning), tuning_variant(opt_tuning),
-                               &L))
+                               &L, tuning_ctas(opt_tuning)))
     return rc;
   Elem* A = reinterpret_cast<Elem*>(d_a);
   Elem* B = reinterpret_cast<Elem*>(d_b);
@@ -362,11 +367,18 @@ int lsb_tune_segmented(const int64_t* h_seg_offsets, int64_t nseg, lsb_tuning_t*
   const int64_t sseg = (int64_t)off.size() - 1;
   if (sn <= 1) return LSB_OK;
   cudaStream_t st = (cudaStream_t)stream;
+  const int cand_bits[] = {8, 11, 16};
+  const int cand_var[] = {0, 2};
   size_t wsb = 0;
-  if (int rc = lsb_segmented_workspace_bytes(sn, sseg, 16, &wsb)) return rc;
-  size_t wsb11 = 0;
-  if (int rc = lsb_segmented_workspace_bytes(sn, sseg, 11, &wsb11)) return rc;
-  wsb = std::max(wsb, wsb11);
+  for (int cb : cand_bits) {
+    size_t x = 0;
+    if (int rc = lsb_segmented_workspace_bytes(sn, sseg, cb, &x)) return rc;
+    wsb = std::max(wsb, x);
+  }
+  DeviceInfo dev;
+  if (int rc = current_device_info(&dev)) return rc;
+  // CTA counts: every resident slot, or one CTA per SM with two-CTA shapes, or half the SMs
+  const int cand_ctas[] = {0, dev.sm_count, std::max(1, dev.sm_count / 2)};
   void *in = nullptr, *a = nullptr, *b = nullptr, *ws = nullptr, *doff = nullptr;
   const size_t bytes = (size_t)sn * sizeof(Elem);
   int rc = LSB_OK;
@@ -385,15 +397,16 @@ int lsb_tune_segmented(const int64_t* h_seg_offsets, int64_t nseg, lsb_tuning_t*
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   if (rc == LSB_OK && (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess))
     rc = LSB_ERR_CUDA;
-  const int cand_bits[] = {8, 11};
-  const int cand_var[] = {0, 2};
   for (int cb : cand_bits) {
     for (int cv : cand_var) {
+     for (int cc : cand_ctas) {
       if (rc != LSB_OK) break;
+      if (cv == 0 && cc == dev.sm_count) continue;  // the variant-0 default is already one CTA per SM
       lsb_tuning_t t;
       std::memset(&t, 0, sizeof t);
       t.digit_bits = cb;
       t.variant = cv;
+      t.ctas = cc;
       float total = 0.f;
       for (int rep = 0; rep < 3 && rc == LSB_OK; rep++) {
         if (cudaMemcpyAsync(a, in, bytes, cudaMemcpyDeviceToDevice, st) != cudaSuccess) rc = LSB_ERR_CUDA;
@@ -411,6 +424,7 @@ int lsb_tune_segmented(const int64_t* h_seg_offsets, int64_t nseg, lsb_tuning_t*
         best_ms = total;
         best = t;
       }
+     }
     }
   }
   if (e0) cudaEventDestroy(e0);
@@ -440,7 +454,7 @@ int lsb_graph_capture_segmented(lsb_elem_t* d_a, lsb_elem_t* d_b, int64_t n_tota
   // resolve device properties and kernel attributes before capturing
   SegLayout L;
   if (int rc = seg_plan_layout(n_total, nseg, tuning_bits(opt_tuning), tuning_variant(opt_tuning),
-                               &L))
+                               &L, tuning_ctas(opt_tuning)))
     return rc;
   if (((uintptr_t)d_workspace & 255u) || workspace_bytes < L.total) return LSB_ERR_WORKSPACE;
   cudaStream_t cs = nullptr;

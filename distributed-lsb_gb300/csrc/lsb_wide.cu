@@ -44,11 +44,12 @@
 
 namespace lsb {
 
-constexpr int kWT = 512;                 // threads per CTA
-constexpr int kWK = 16;                  // items per thread
-constexpr uint32_t kWE = kWT * kWK;      // elements per tile (A and B)
-constexpr int kWW = kWT / 32;
-constexpr int kWWP = kWW + 1;            // padded counter row (distinct banks per lane)
+constexpr int kCW = 16;                  // compute warps per CTA
+constexpr uint32_t kCT = kCW * 32;       // compute threads
+constexpr int kWT = kCT + 32;            // + one producer warp
+constexpr int kWK = 12;                  // items per compute thread
+constexpr uint32_t kWE = kCT * kWK;      // elements per tile (A and B): 6144
+constexpr int kWWP = kCW + 1;            // padded counter row (distinct banks per lane)
 constexpr uint32_t kPTS = 264;           // piece-table row: 257 u16 starts, padded to 16 B
 constexpr uint32_t kFirstStride = 264;   // per-slot B-tile numbering: 257 u32
 constexpr uint32_t kNone = 0, kItemA = 1, kItemB = 2, kDone = 3;
@@ -81,7 +82,15 @@ struct WideArgs {
   uint16_t* PT;       // [NZ][M][kPTS] start of each h inside each tile
   uint64_t* status;   // [NZ][nbmax][256] look-back statuses of B tiles
   uint32_t M, NZ, K, nbmax, totalA;
+  int prof;           // record per-phase cycles into ctrl->wide_prof
 };
+
+// Phases of ctrl->wide_prof[pass][*] (diagnostics; thread 0 of every CTA).
+//   0  compute warps: cycles waiting for their next tile to be loaded
+//   1  compute warps: cycles in A tiles      2  compute warps: cycles in B tiles
+//   4  producer: cycles choosing work        5  producer: B prefix prefetch (incl. waits)
+//   7  A tiles loaded    8  B tiles loaded    9  producer polls that found nothing to do
+//  10  producer: cycles from kernel start to end
 
 __device__ __forceinline__ uint32_t ld_relaxed_u16(const uint16_t* p) {
   unsigned short v;
@@ -194,7 +203,7 @@ __device__ __forceinline__ void byte_flush(const uint32_t* words, uint32_t* g) {
 // histogram of ND 16-bit digits, one read of the keys
 
 constexpr int kH16Threads = 512;
-constexpr int kH16Unroll = 4;
+constexpr int kH16Unroll = 8;
 
 template <int ND>
 __global__ void __launch_bounds__(kH16Threads)
@@ -246,15 +255,169 @@ __global__ void __launch_bounds__(kH16Threads)
   for (int dd = 0; dd < ND; dd++) byte_flush(cw + dd * 16384, ghist + (size_t)dd * 65536u);
 }
 
+// ---------------------------------------------------------------------------
+// histogram of four 16-bit digits in one read: a cluster of two CTAs, each
+// holding the byte counters of two digits (128 KiB), fed by multicast bulk
+// copies so that every key is read from memory once and lands in both CTAs'
+// shared memory
+
+constexpr int kHCThreads = 512;
+constexpr uint32_t kHCStage = 1024;  // elements per stage (16 KiB)
+constexpr int kHCStages = 4;
+
+__device__ __forceinline__ uint32_t cluster_ctarank() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+// the same shared-memory offset in CTA `rank` of the cluster
+__device__ __forceinline__ uint32_t map_shared(uint32_t addr, uint32_t rank) {
+  uint32_t r;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(addr), "r"(rank));
+  return r;
+}
+__device__ __forceinline__ void mbar_arrive_cluster(uint32_t cluster_addr) {
+  asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];" ::"r"(cluster_addr)
+               : "memory");
+}
+// bulk copy of `bytes` from global memory into the same offset of every CTA
+// in `mask`, completing on each one's barrier at offset `bar`
+__device__ __forceinline__ void bulk_g2s_multicast(uint32_t dst, const void* src, uint32_t bytes,
+                                                   uint32_t bar, uint16_t mask) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes.multicast::cluster"
+      " [%0], [%1], %2, [%3], %4;" ::"r"(dst),
+      "l"(src), "r"(bytes), "r"(bar), "h"(mask)
+      : "memory");
+}
+__device__ __forceinline__ void cluster_sync_all() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\nbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+
+__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kHCThreads, 1)
+    k_hist16_cluster(const Elem* __restrict__ data, uint32_t n, int first_digit,
+                     uint32_t* __restrict__ ghist, Ctrl* ctrl) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  uint32_t* cw = reinterpret_cast<uint32_t*>(smem);                           // [2][16384]
+  Elem* stage = reinterpret_cast<Elem*>(smem + 2u * 16384u * 4u);             // [kHCStages][kHCStage]
+  __shared__ __align__(8) uint64_t s_full[kHCStages], s_empty[kHCStages];
+  __shared__ uint32_t s_bad;
+  const uint32_t rank = cluster_ctarank(), peer = rank ^ 1u;
+  const uint32_t lane = lane_id();
+  for (uint32_t i = threadIdx.x; i < 2u * 16384u; i += blockDim.x) cw[i] = 0u;
+  if (threadIdx.x == 0) {
+    s_bad = 0u;
+    for (int b = 0; b < kHCStages; b++) {
+      mbar_init(smem_u32(&s_full[b]), 1);   // this CTA's expect_tx arrival (+ both halves' bytes)
+      mbar_init(smem_u32(&s_empty[b]), 2);  // both CTAs' consumers
+    }
+    fence_mbar_init();
+  }
+  __syncthreads();
+  cluster_sync_all();  // both CTAs' barriers exist before any copy or remote arrival
+  // this cluster's contiguous range of elements
+  const uint32_t clusters = gridDim.x / 2u, c = blockIdx.x / 2u;
+  const uint64_t per = ((uint64_t)n + clusters - 1) / clusters;
+  const uint64_t lo64 = (uint64_t)c * per, hi64 = lo64 + per;
+  const uint32_t lo = (uint32_t)(lo64 < n ? lo64 : n);
+  const uint32_t hi = (uint32_t)(hi64 < n ? hi64 : n);
+  const uint32_t nst = (hi - lo + kHCStage - 1) / kHCStage;
+  auto stage_len = [&](uint32_t i) { return min(kHCStage, hi - lo - i * kHCStage); };
+  // thread 0: this CTA's half of stage i into buffer i % kHCStages of both CTAs
+  auto issue = [&](uint32_t i) {
+    const uint32_t b = i % kHCStages, len = stage_len(i);
+    const uint32_t half = min(len, kHCStage / 2u);
+    const uint32_t e0 = rank == 0 ? 0u : half, e1 = rank == 0 ? half : len;
+    const uint32_t full = smem_u32(&s_full[b]);
+    mbar_arrive_expect_tx(full, len * (uint32_t)sizeof(Elem));
+    if (e1 > e0)
+      bulk_g2s_multicast(smem_u32(stage + (size_t)b * kHCStage + e0), data + lo + (size_t)i * kHCStage + e0,
+                         (e1 - e0) * (uint32_t)sizeof(Elem), full, (uint16_t)0x3);
+  };
+  if (threadIdx.x == 0)
+    for (uint32_t i = 0; i < nst && i < (uint32_t)kHCStages; i++) issue(i);
+  uint32_t* g0 = ghist + (size_t)(2u * rank) * 65536u;
+  for (uint32_t i = 0; i < nst; i++) {
+    const uint32_t b = i % kHCStages, len = stage_len(i);
+    const bool ok = mbar_wait_bounded(smem_u32(&s_full[b]), (i / kHCStages) & 1u);
+    if (!ok) atomicOr(&s_bad, 1u);
+    __syncthreads();
+    if (s_bad) break;
+    const Elem* st = stage + (size_t)b * kHCStage;
+#pragma unroll
+    for (uint32_t q = 0; q < kHCStage / kHCThreads; q++) {
+      const uint32_t pos = q * kHCThreads + threadIdx.x;  // a warp reads 32 consecutive elements
+      const bool valid = pos < len;
+      const uint64_t key = valid ? st[pos].key : 0ull;
+      if (__all_sync(0xffffffffu, valid)) {
+        const uint64_t x = key ^ __shfl_sync(0xffffffffu, key, 0);
+        const uint64_t diff = ((uint64_t)__reduce_or_sync(0xffffffffu, (uint32_t)(x >> 32)) << 32) |
+                              __reduce_or_sync(0xffffffffu, (uint32_t)x);
+#pragma unroll
+        for (int dd = 0; dd < 2; dd++) {
+          const int shift = 16 * (first_digit + 2 * (int)rank + dd);
+          const uint32_t d = digit_of(key, shift, 0xFFFFu);
+          if (digit_of(diff, shift, 0xFFFFu) == 0u) {
+            if (lane == 0) byte_count(cw + dd * 16384, d, 32u, g0 + (size_t)dd * 65536u);
+          } else {
+            byte_count(cw + dd * 16384, d, 1u, g0 + (size_t)dd * 65536u);
+          }
+        }
+      } else if (valid) {
+#pragma unroll
+        for (int dd = 0; dd < 2; dd++)
+          byte_count(cw + dd * 16384, digit_of(key, 16 * (first_digit + 2 * (int)rank + dd), 0xFFFFu), 1u,
+                     g0 + (size_t)dd * 65536u);
+      }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      // both consumers (this CTA and its peer) are done with buffer b
+      const uint32_t e = smem_u32(&s_empty[b]);
+      mbar_arrive_cluster(map_shared(e, rank));
+      mbar_arrive_cluster(map_shared(e, peer));
+      if (i + kHCStages < nst) {
+        // refill it once the peer is done with it too
+        if (!mbar_wait_bounded(e, (i / kHCStages) & 1u)) atomicOr(&s_bad, 1u);
+        else issue(i + kHCStages);
+      }
+    }
+  }
+  if (s_bad) record_error(ctrl, kStatusTimeout, kWhereBulkCopy);
+  __syncthreads();
+  // no CTA leaves while its peer may still copy into it or arrive on its barriers
+  cluster_sync_all();
+  byte_flush(cw, g0);
+  byte_flush(cw + 16384, g0 + 65536u);
+}
+
 // Counts of 16-bit digits [first_digit, first_digit + num_digits) into
-// d_counts[num_digits][65536] (uint32; zeroed here). Reads the keys once per
-// three digits.
+// d_counts[num_digits][65536] (uint32; zeroed here). Four digits: one read of
+// the keys by clusters of two CTAs; otherwise one read per three digits.
+static bool hist16_cluster_enabled() {
+  const char* e = std::getenv("LSB_HIST16_CLUSTER");
+  return !(e && e[0] == '0');
+}
+
 int hist16(const Elem* data, uint32_t n, int first_digit, int num_digits, uint32_t* d_counts,
-           cudaStream_t st) {
+           cudaStream_t st, Ctrl* ctrl) {
   DeviceInfo dev;
   if (int rc = current_device_info(&dev)) return rc;
   if (cudaMemsetAsync(d_counts, 0, (size_t)num_digits * 65536u * 4u, st) != cudaSuccess) return 5;
   if (n == 0) return 0;
+  if (num_digits == 4 && ctrl && hist16_cluster_enabled() && dev.sm_count >= 2) {
+    const size_t smem = 2u * 65536u + (size_t)kHCStages * kHCStage * sizeof(Elem);
+    if (cudaFuncSetAttribute(k_hist16_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) ==
+        cudaSuccess) {
+      // one cluster of two CTAs per pair of SMs, no more than the work needs
+      const uint64_t want = ((uint64_t)n + 4u * kHCStage - 1) / (4u * kHCStage);
+      const uint32_t clusters = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(want, (uint64_t)dev.sm_count / 2u));
+      ProfScope prof("hist16", st);
+      k_hist16_cluster<<<2u * clusters, kHCThreads, smem, st>>>(data, n, first_digit, d_counts, ctrl);
+      if (cudaPeekAtLastError() == cudaSuccess) return 0;
+    }
+    cudaGetLastError();  // no cluster launch here: count with the per-CTA kernels
+  }
   for (int d0 = 0; d0 < num_digits; d0 += 3) {
     const int nd = std::min(3, num_digits - d0);
     auto kern = nd == 3 ? k_hist16<3> : nd == 2 ? k_hist16<2> : k_hist16<1>;
@@ -278,372 +441,682 @@ int hist16(const Elem* data, uint32_t n, int first_digit, int num_digits, uint32
 }
 
 // ---------------------------------------------------------------------------
-// the pass
+// pass plan for 16-bit digits: exclusive digit starts (the global scan of
+// GlobalCounts, mpi/mpi_lsbsort.cpp:397-426), constant digits, buffer parity
 
-// Stable rank of each item's 8-bit digit inside its warp (peers from ballots,
-// per-warp counters [256][kWWP], zero on entry); then per-digit totals of the
-// tile (tcount), tile-local starts (tstart) and per-(digit, warp) starts
-// written back into the counters. Items with dg == kSent are not counted.
-template <bool FULL>
-__device__ __forceinline__ void rank_tile(const uint32_t (&dg)[kWK], uint32_t (&r)[kWK],
-                                          uint32_t* wcnt, uint32_t* tcount, uint32_t* tstart,
-                                          uint32_t* s_wt) {
-  constexpr uint32_t kSent = 0xffffffffu;
-  const uint32_t warp = threadIdx.x >> 5, lt = lanemask_lt();
-#pragma unroll
-  for (int q = 0; q < kWK; q++) {
-    const bool valid = FULL || dg[q] != kSent;
-    const uint32_t peers = FULL ? warp_peers_fixed<8>(dg[q]) : warp_peers(dg[q], 8, valid);
-    uint32_t c = 0;
-    if (valid) c = wcnt[dg[q] * kWWP + warp];
-    r[q] = c + __popc(peers & lt);
-    __syncwarp();
-    if (valid) wcnt[dg[q] * kWWP + warp] = c + __popc(peers);  // every peer writes the same count
-    __syncwarp();
+constexpr int kPlan16Threads = 1024;
+
+// One CTA per digit: 64 rounds of 1024 consecutive bins, each round read
+// coalesced and scanned across the CTA, the running total carried on.
+__global__ void __launch_bounds__(kPlan16Threads)
+    k_plan16_scan(const uint32_t* __restrict__ ghist, uint32_t* __restrict__ gstart, uint32_t n,
+                  Ctrl* ctrl) {
+  __shared__ uint32_t s_wt[33];
+  __shared__ uint32_t s_const;
+  const uint32_t p = blockIdx.x;
+  const uint32_t* c = ghist + (size_t)p * 65536u;
+  uint32_t* g = gstart + (size_t)p * 65536u;
+  if (threadIdx.x == 0) s_const = 0u;
+  uint32_t carry = 0;
+  for (uint32_t r = 0; r < 65536u; r += kPlan16Threads) {
+    const uint32_t v = c[r + threadIdx.x];
+    if (v == n) s_const = 1u;
+    uint32_t tot;
+    const uint32_t ex = block_exclusive_scan(v, s_wt, &tot);
+    g[r + threadIdx.x] = carry + ex;
+    carry += tot;
   }
   __syncthreads();
+  if (threadIdx.x == 0 && s_const) {
+    if (p < 32) atomicOr(&ctrl->skip_mask_lo, 1u << p);
+    else atomicOr(&ctrl->skip_mask_hi, 1u << (p - 32));
+  }
+}
+
+// Buffer parity of every pass from the constant digits, and whether the
+// result needs a copy back (one thread).
+__global__ void k_plan16_parity(int num_digits, int target_parity, int api_bits, uint32_t n,
+                                Ctrl* ctrl) {
+  if (threadIdx.x != 0) return;
+  uint32_t par = 0, runs = 0;
+  for (int p = 0; p < num_digits; p++) {
+    ctrl->parity[p] = par;
+    const uint32_t m = p < 32 ? ctrl->skip_mask_lo : ctrl->skip_mask_hi;
+    if (!((m >> (p & 31)) & 1u)) {
+      par ^= 1u;
+      runs++;
+    }
+  }
+  ctrl->parity[num_digits] = par;
+  ctrl->passes_run = runs;
+  ctrl->num_passes = (uint32_t)num_digits;
+  ctrl->final_copy = (par != (uint32_t)target_parity) ? 1u : 0u;
+  ctrl->api_bits = (uint32_t)api_bits;
+  ctrl->sub = 1u;
+  ctrl->n = n;
+}
+
+// ---------------------------------------------------------------------------
+// the pass: one producer warp (choice of work, bulk-copy loads and gathers
+// into shared memory, prefetch of each bucket's running prefix and digit
+// starts, the stores) and kCW compute warps (ranking and staging), over two
+// tile buffers in shared memory, so that a tile's memory traffic overlaps the
+// ranking of the tile before it
+
+// Per-buffer description of the tile it holds, written by the producer
+// before it releases the buffer's full barrier.
+struct ItemDesc {
+  uint32_t kind;     // kItemA, kItemB or kDone
+  uint32_t k, j;     // chunk; A: tile of the chunk, B: B tile of the chunk
+  uint32_t len;      // elements in the tile
+  uint32_t h, i, J;  // B: bucket, tile of the bucket, tiles of the bucket
+  uint32_t pad;
+};
+
+__device__ __forceinline__ void compute_sync() {
+  asm volatile("bar.sync 1, %0;" ::"n"(kCT) : "memory");
+}
+// barrier of the compute warps that returns whether any of them passed `p`
+__device__ __forceinline__ bool compute_sync_or(bool p) {
+  uint32_t r;
+  asm volatile(
+      "{\n .reg .pred a, b;\n setp.ne.u32 a, %1, 0;\n barrier.red.or.pred b, 1, %2, a;\n"
+      " selp.u32 %0, 1, 0, b;\n}\n"
+      : "=r"(r)
+      : "r"((uint32_t)p), "n"(kCT)
+      : "memory");
+  return r != 0;
+}
+// exclusive scan of one value per compute thread (compute warps only)
+__device__ __forceinline__ uint32_t compute_exclusive_scan(uint32_t v, uint32_t* warp_tot,
+                                                           uint32_t* total) {
+  const uint32_t lane = lane_id(), warp = threadIdx.x >> 5;
+  uint32_t x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= (uint32_t)o) x += y;
+  }
+  if (lane == 31) warp_tot[warp] = x;
+  compute_sync();
+  if (warp == 0) {
+    const uint32_t t = lane < (uint32_t)kCW ? warp_tot[lane] : 0u;
+    uint32_t s = t;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, s, o);
+      if (lane >= (uint32_t)o) s += y;
+    }
+    if (lane < (uint32_t)kCW) warp_tot[lane] = s - t;
+    if (lane == (uint32_t)kCW - 1) warp_tot[32] = s;
+  }
+  compute_sync();
+  const uint32_t r = warp_tot[warp] + x - v;
+  *total = warp_tot[32];
+  compute_sync();
+  return r;
+}
+__device__ __forceinline__ bool mbar_test_wait(uint32_t bar, uint32_t phase) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(bar), "r"(phase)
+      : "memory");
+  return ok != 0;
+}
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ void bulk_wait_read_one() {
+  asm volatile("cp.async.bulk.wait_group.read 1;" ::: "memory");
+}
+__device__ __forceinline__ void bulk_wait_one() {
+  asm volatile("cp.async.bulk.wait_group 1;" ::: "memory");
+}
+
+// Stable rank of each item's 8-bit digit inside its warp (peers from ballots,
+// per-warp counters [256][kWWP], zero on entry), then the tile's per-digit
+// totals (tcount), tile-local starts (tstart) and per-(digit, warp) starts
+// written back into the counters. Items with dg == kSent are not counted.
+// Compute warps only.
+// The digit of item q is (v[q].key >> dshift) & 0xff, recomputed where it is
+// needed rather than kept in registers; item q of lane l in warp w is tile
+// position w*32*kWK + q*32 + l, valid below len.
+template <bool FULL>
+__device__ __forceinline__ void rank_tile(const Elem (&v)[kWK], int dshift, uint32_t len,
+                                          uint32_t (&r)[kWK], uint32_t* wcnt, uint32_t* tcount,
+                                          uint32_t* tstart, uint32_t* s_wt) {
+  const uint32_t warp = threadIdx.x >> 5, lt = lanemask_lt();
+  const uint32_t base = warp * 32u * kWK + lane_id();
+#pragma unroll
+  for (int q = 0; q < kWK; q++) {
+    const bool valid = FULL || base + (uint32_t)q * 32u < len;
+    const uint32_t dg = digit_of(v[q].key, dshift, 0xFFu);
+    const uint32_t peers = FULL ? warp_peers_fixed<8>(dg) : warp_peers(dg, 8, valid);
+    uint32_t c = 0;
+    if (valid) c = wcnt[dg * kWWP + warp];
+    r[q] = c + __popc(peers & lt);
+    __syncwarp();
+    if (valid) wcnt[dg * kWWP + warp] = c + __popc(peers);  // every peer writes the same count
+    __syncwarp();
+  }
+  compute_sync();
   const uint32_t b = threadIdx.x;
   uint32_t sum = 0;
   if (b < 256u) {
 #pragma unroll
-    for (int w = 0; w < kWW; w++) sum += wcnt[b * kWWP + w];
+    for (int w = 0; w < kCW; w++) sum += wcnt[b * kWWP + w];
     tcount[b] = sum;
   }
   uint32_t tot;
-  uint32_t off = block_exclusive_scan(sum, s_wt, &tot);
+  uint32_t off = compute_exclusive_scan(sum, s_wt, &tot);
   if (b < 256u) {
     tstart[b] = off;
 #pragma unroll
-    for (int w = 0; w < kWW; w++) {
+    for (int w = 0; w < kCW; w++) {
       const uint32_t c = wcnt[b * kWWP + w];
       wcnt[b * kWWP + w] = off;
       off += c;
     }
   }
-  __syncthreads();
+  compute_sync();
 }
 
-// Stages this thread's items in digit order, then clears its warp's counter
-// column for the next tile (only this warp reads the column while staging).
-__device__ __forceinline__ void stage_tile(const Elem (&v)[kWK], const uint32_t (&dg)[kWK],
-                                           const uint32_t (&r)[kWK], uint32_t* wcnt, Elem* buf) {
-  const uint32_t warp = threadIdx.x >> 5, lane = lane_id();
-#pragma unroll
-  for (int q = 0; q < kWK; q++)
-    if (dg[q] != 0xffffffffu) buf[r[q] + wcnt[dg[q] * kWWP + warp]] = v[q];
-  fence_proxy_async_smem();
-  __syncwarp();
-  for (uint32_t b = lane; b < 256u; b += 32u) wcnt[b * kWWP + warp] = 0u;
-}
-
+// 17 warps: the register file is split over the SM's four schedulers, so
+// one of them holds five warps and the kernel gets at most 96 registers per
+// thread.
 __global__ void __launch_bounds__(kWT, 1)
     k_wide(Elem* __restrict__ X, Elem* __restrict__ Y, uint32_t n, int pass, int digit,
            const uint32_t* __restrict__ gstart, WideArgs w, Ctrl* ctrl) {
   constexpr uint32_t kSent = 0xffffffffu;
   extern __shared__ __align__(16) unsigned char smem[];
-  __shared__ __align__(8) uint64_t s_bar;
+  __shared__ __align__(8) uint64_t s_full[2], s_staged[2];
+  __shared__ ItemDesc s_desc[2];
   __shared__ uint32_t s_wt[33];
-  __shared__ uint32_t s_kind, s_a, s_k, s_j, s_h, s_i, s_J, s_flag;
+  __shared__ uint32_t s_first[260], s_size[256];  // producer: plan of its current B chunk
+  __shared__ unsigned long long s_prof[12];
 
   if (pass_skipped(ctrl, pass)) return;
-  Elem* buf = reinterpret_cast<Elem*>(smem);                                   // [kWE]
-  uint32_t* wcnt = reinterpret_cast<uint32_t*>(smem + (size_t)kWE * sizeof(Elem));  // [256][kWWP]
-  uint32_t* tcount = wcnt + 256 * kWWP;                                        // [256]
-  uint32_t* tstart = tcount + 256;                                             // [256]
-  uint32_t* gbase = tstart + 256;                                              // [256]
+  Elem* bufs = reinterpret_cast<Elem*>(smem);                                       // [2][kWE]
+  uint32_t* wcnt = reinterpret_cast<uint32_t*>(smem + 2u * kWE * sizeof(Elem));     // [256][kWWP]
+  uint32_t* tcount = wcnt + 256 * kWWP;  // [2][256] per-digit counts of the tile in each buffer
+  uint32_t* tstart = tcount + 512;       // [2][256] tile-local start of each digit
+  uint32_t* gbase = tstart + 512;        // [2][256] B: destination of each digit's run
+  uint32_t* pre = gbase + 512;           // [2][256] B: running prefix R[h][l] (first tile of a bucket)
+  uint32_t* gst = pre + 512;             // [2][256] B: digit starts start(h, l)
+  uint32_t* nx_pre = gst + 512;          // [256] producer: R[h][l] of the next B tile, staged
+  uint32_t* nx_gst = nx_pre + 256;       // [256] producer: start(h, l) of the next B tile, staged
 
   const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = lane_id();
   const uint32_t par = ctrl->parity[pass];
   const Elem* __restrict__ src = par ? Y : X;
   Elem* __restrict__ dst = par ? X : Y;
   const int shift = 16 * digit;
-  const uint32_t bar = smem_u32(&s_bar);
   const size_t C = (size_t)w.M * kWE;
+  const bool prof = w.prof != 0 && pass < 4;
 
   for (uint32_t i = tid; i < 256u * kWWP; i += kWT) wcnt[i] = 0u;
+  if (tid < 12u) s_prof[tid] = 0ull;
   if (tid == 0) {
-    mbar_init(bar, 1);
+    for (int b = 0; b < 2; b++) {
+      mbar_init(smem_u32(&s_full[b]), 2);    // the producer's two arrivals (+ copied bytes)
+      mbar_init(smem_u32(&s_staged[b]), 1);  // compute thread 0
+    }
     fence_mbar_init();
   }
   __syncthreads();
+  const long long t_start = clock64();
 
-  uint32_t phase = 0;
-  bool gather_pending = false;  // bulk copies into the buffer not yet seen complete
-  uint32_t held_a = kSent;  // thread 0: an A tile taken whose Z slot was not free yet
-  uint32_t idle = 0, ns = 8;
-  int32_t pending = -1;     // chunk of this CTA's last A tile, completion not yet signalled
+  if (warp == (uint32_t)kCW) {
+    // =================== producer warp ===================
+    uint32_t held_a = kSent;               // lane 0: A tile taken whose Z slot was not free yet
+    uint32_t cb_k = 0, cb_nb = 0;          // lane 0: current B chunk and its B tile count
+    bool cb_ready = false;
+    uint32_t plan_k = kSent;               // chunk whose plan is in s_first / s_size
+    uint32_t it_load = 0, it_store = 0;    // next item to load / to store
+    int32_t pend_a = -1;                   // chunk of an A tile whose stores are in the
+                                           // newest bulk group, signalled once complete
+    int32_t pend_a_old = -1;               // the same for the group before it
+    bool done = false, failed = false;
+    uint32_t idle = 0, ns = 8;
+    // the item chosen for loading (uniform across the warp)
+    ItemDesc nx;
+    bool have_nx = false, nx_pre_ok = false;
+    long long t_mark = clock64();
+    auto pmark = [&](int f) {
+      if (prof && lane == 0) {
+        const long long now = clock64();
+        s_prof[f] += (unsigned long long)(now - t_mark);
+        t_mark = now;
+      }
+    };
 
-  // chunk k's tile count
-  auto chunk_tiles = [&](uint32_t k) { return min(w.M, w.totalA - k * w.M); };
+    auto chunk_tiles = [&](uint32_t k) { return min(w.M, w.totalA - k * w.M); };
 
-  // B tile numbering of chunk k, once all its A tiles are done: bucket h gets
-  // ceil(S[k][h] / kWE) tiles (none when empty). CTA-wide.
-  auto build_plan = [&](uint32_t k) {
-    const uint32_t s = k % w.NZ;
-    if (tid == 0) __threadfence();  // acquire: the other A tiles' bucket counts
-    __syncthreads();
-    uint32_t J = 0;
-    if (tid < 256u) J = (ld_relaxed_u32(&w.S[(size_t)k * 256u + tid]) + kWE - 1u) / kWE;
-    uint32_t tot;
-    const uint32_t ex = block_exclusive_scan(J, s_wt, &tot);
-    if (tid < 256u) st_relaxed_u32(&w.first[s * kFirstStride + tid], ex);
-    if (tid == 0) {
-      st_relaxed_u32(&w.first[s * kFirstStride + 256u], tot);
-      st_relaxed_u32(&w.chunks[k].nb, tot);
-    }
-    __syncthreads();
-    if (tid == 0) {
-      __threadfence();
-      st_release_u32(&w.chunks[k].plan_ready, 1u);
-    }
-  };
-
-  // Signals that this CTA's last A tile is complete in Z (its bulk copies are
-  // done). CTA-wide; builds the chunk's plan if that tile was its last one.
-  auto flush = [&]() {
-    if (pending < 0) return;
-    if (tid < 4u) {
-      bulk_wait_all();
+    // Signals that a chunk's A tile is complete in Z (its stores finished);
+    // the chunk's last one also publishes the chunk's plan.
+    auto signal_a = [&](uint32_t k) {
       fence_proxy_async_global();
-    }
-    __syncthreads();
-    if (tid == 0) {
       __threadfence();
-      const uint32_t k = (uint32_t)pending;
-      s_flag = atomicAdd(&w.chunks[k].adone, 1u) + 1u == chunk_tiles(k) ? 1u : 0u;
-    }
-    __syncthreads();
-    if (s_flag) build_plan((uint32_t)pending);
-    pending = -1;
-  };
+      __syncwarp();
+      uint32_t last = 0;
+      if (lane == 0) last = atomicAdd(&w.chunks[k].adone, 1u) + 1u == chunk_tiles(k) ? 1u : 0u;
+      last = __shfl_sync(0xffffffffu, last, 0);
+      if (!last) return;
+      __threadfence();  // acquire: the other A tiles' bucket counts
+      const uint32_t s = k % w.NZ;
+      uint32_t Jl[8], sum = 0;
+#pragma unroll
+      for (int r = 0; r < 8; r++) {
+        Jl[r] = (ld_relaxed_u32(&w.S[(size_t)k * 256u + lane * 8u + r]) + kWE - 1u) / kWE;
+        sum += Jl[r];
+      }
+      uint32_t x = sum;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= (uint32_t)o) x += y;
+      }
+      uint32_t ex = x - sum;
+#pragma unroll
+      for (int r = 0; r < 8; r++) {
+        st_relaxed_u32(&w.first[s * kFirstStride + lane * 8u + r], ex);
+        ex += Jl[r];
+      }
+      if (lane == 31) {
+        st_relaxed_u32(&w.first[s * kFirstStride + 256u], x);
+        st_relaxed_u32(&w.chunks[k].nb, x);
+      }
+      __threadfence();
+      __syncwarp();
+      if (lane == 0) st_release_u32(&w.chunks[k].plan_ready, 1u);
+    };
+    // all bulk groups complete: signal every pending A tile
+    auto drain = [&]() {
+      bulk_wait_all();
+      __syncwarp();
+      if (pend_a_old >= 0) signal_a((uint32_t)pend_a_old);
+      if (pend_a >= 0) signal_a((uint32_t)pend_a);
+      pend_a = pend_a_old = -1;
+    };
 
-  // thread 0: the next item, without waiting (kNone if nothing is runnable now)
-  auto try_pick = [&]() -> uint32_t {
-    if (error_raised(ctrl)) return kDone;
-    uint32_t kb = ld_acquire_u32(&w.ctl->bchunk);
-    while (kb < w.K) {
-      if (!ld_acquire_u32(&w.chunks[kb].plan_ready)) break;
-      const uint32_t j = atomicAdd(&w.chunks[kb].bticket, 1u);
-      if (j < ld_relaxed_u32(&w.chunks[kb].nb)) {
-        s_k = kb;
-        s_j = j;
-        return kItemB;
+    // lane 0: the next item, without waiting (kNone if nothing is runnable now)
+    auto try_pick = [&](ItemDesc& d) -> uint32_t {
+      if (error_raised(ctrl)) return kDone;
+      for (;;) {
+        if (cb_k >= w.K) break;
+        if (!cb_ready) {
+          if (!ld_acquire_u32(&w.chunks[cb_k].plan_ready)) break;
+          cb_nb = ld_relaxed_u32(&w.chunks[cb_k].nb);
+          cb_ready = true;
+        }
+        const uint32_t j = atomicAdd(&w.chunks[cb_k].bticket, 1u);
+        if (j < cb_nb) {
+          d.kind = kItemB;
+          d.k = cb_k;
+          d.j = j;
+          return kItemB;
+        }
+        atomicCAS(&w.ctl->bchunk, cb_k, cb_k + 1u);
+        cb_k = max(cb_k + 1u, ld_acquire_u32(&w.ctl->bchunk));
+        cb_ready = false;
       }
-      atomicCAS(&w.ctl->bchunk, kb, kb + 1u);
-      kb = ld_acquire_u32(&w.ctl->bchunk);
-    }
-    if (held_a == kSent && ld_relaxed_u32(&w.ctl->aticket) < w.totalA) {
-      const uint32_t a = atomicAdd(&w.ctl->aticket, 1u);
-      if (a < w.totalA) held_a = a;
-    }
-    if (held_a != kSent) {
-      const uint32_t k = held_a / w.M;
-      bool free_slot = k < w.NZ;
-      if (!free_slot) {
-        const uint32_t kp = k - w.NZ;  // the chunk that used the slot before
-        free_slot = ld_acquire_u32(&w.chunks[kp].plan_ready) &&
-                    ld_acquire_u32(&w.chunks[kp].bdone) == ld_relaxed_u32(&w.chunks[kp].nb);
+      if (held_a == kSent && ld_relaxed_u32(&w.ctl->aticket) < w.totalA) {
+        const uint32_t a = atomicAdd(&w.ctl->aticket, 1u);
+        if (a < w.totalA) held_a = a;
       }
-      if (free_slot) {
-        s_a = held_a;
+      if (held_a != kSent) {
+        const uint32_t k = held_a / w.M;
+        bool free_slot = k < w.NZ;
+        if (!free_slot) {
+          const uint32_t kp = k - w.NZ;  // the chunk that used the slot before
+          free_slot = ld_acquire_u32(&w.chunks[kp].plan_ready) &&
+                      ld_acquire_u32(&w.chunks[kp].bdone) == ld_relaxed_u32(&w.chunks[kp].nb);
+        }
+        if (!free_slot) return kNone;
+        d.kind = kItemA;
+        d.k = k;
+        d.j = held_a % w.M;
+        d.len = min(kWE, n - held_a * kWE);
         held_a = kSent;
         return kItemA;
       }
-      return kNone;
-    }
-    return kb >= w.K ? kDone : kNone;
-  };
+      return cb_k >= w.K ? kDone : kNone;
+    };
 
-  for (;;) {
-    if (tid == 0) {
-      uint32_t kind = try_pick();
-      if (kind == kNone && pending < 0) {
-        if (++idle >= kSpinLimit || ((idle & 63u) == 0u && error_raised(ctrl))) {
-          record_error(ctrl, kStatusTimeout, kWhereSchedule);
-          kind = kDone;
-        } else {
-          __nanosleep(ns);
-          if (ns < 256) ns <<= 1;
+    // B tile (k, j): bucket, its size and the running-prefix prefetch. Returns
+    // false while the bucket's earlier chunk has not folded its counts yet.
+    auto prepare_b = [&](ItemDesc& d) -> bool {
+      const uint32_t s = d.k % w.NZ;
+      if (plan_k != d.k) {
+        for (uint32_t x = lane; x < 257u; x += 32u) s_first[x] = ld_relaxed_u32(&w.first[s * kFirstStride + x]);
+        for (uint32_t x = lane; x < 256u; x += 32u) s_size[x] = ld_relaxed_u32(&w.S[(size_t)d.k * 256u + x]);
+        __syncwarp();
+        plan_k = d.k;
+      }
+      uint32_t hit = 0, hh = 0;
+#pragma unroll
+      for (int r = 0; r < 8; r++) {
+        const uint32_t x = lane * 8u + r;
+        if (s_first[x] <= d.j && d.j < s_first[x + 1]) {
+          hit = 1;
+          hh = x;
         }
-      } else if (kind != kNone) {
-        idle = 0;
-        ns = 8;
       }
-      s_kind = kind;
-    }
-    __syncthreads();
-    const uint32_t kind = s_kind;
-    if (kind == kDone) break;
-    if (kind == kNone) {  // nothing runnable: let this CTA's own A tile count first
-      flush();
-      continue;
-    }
-    // the previous item's bulk copies must have read the buffer before it is reused
-    bulk_wait_read_all();
+      const uint32_t src_lane = __ffs(__ballot_sync(0xffffffffu, hit)) - 1u;
+      d.h = __shfl_sync(0xffffffffu, hh, src_lane);
+      d.i = d.j - s_first[d.h];
+      d.J = s_first[d.h + 1] - s_first[d.h];
+      const uint32_t lo = d.i * kWE;
+      d.len = min(kWE, s_size[d.h] - lo);
+      // digit starts, and the running prefix for the bucket's first tile
+      bool ok = true;
+      if (d.i == 0) {
+        uint32_t kp = kSent;
+        if (lane == 0) {
+          int32_t q = (int32_t)d.k - 1;
+          while (q >= 0 && ld_relaxed_u32(&w.S[(size_t)q * 256u + d.h]) == 0u) q--;
+          kp = q < 0 ? kSent : (uint32_t)q;
+          ok = kp == kSent || ld_acquire_u32(&w.epoch[d.h]) >= kp + 1u;
+        }
+        ok = __shfl_sync(0xffffffffu, (uint32_t)ok, 0) != 0;
+        if (!ok) return false;
+        __syncwarp();
+      }
+#pragma unroll
+      for (int r = 0; r < 8; r++) {
+        const uint32_t l = lane + 32u * r;
+        nx_pre[l] = d.i == 0 ? ld_relaxed_u32(&w.R[d.h * 256u + l]) : 0u;
+        nx_gst[l] = gstart[(d.h << 8) | l];
+      }
+      return true;
+    };
 
-    Elem v[kWK];
-    uint32_t dg[kWK], r[kWK];
-    if (kind == kItemA) {
-      // ---- A: sort one input tile by the high byte into its chunk's Z slot
-      const uint32_t a = s_a, k = a / w.M, t = a % w.M, s = k % w.NZ;
-      const uint32_t begin = a * kWE, len = min(kWE, n - begin);
-      const bool full = len == kWE;
-      const Elem* p = src + begin + warp * 32u * kWK + lane;
+    // bulk copies of item d into buffer b (after the buffer's last stores have read it)
+    auto issue_load = [&](const ItemDesc& d, uint32_t b) {
+      const uint32_t full = smem_u32(&s_full[b]);
+      Elem* tb = bufs + (size_t)b * kWE;
+      const uint32_t s = d.k % w.NZ;
+      if (lane == 0) mbar_arrive_expect_tx(full, d.len * (uint32_t)sizeof(Elem));
+      __syncwarp();
+      fence_proxy_async_global();
+      if (d.kind == kItemA) {
+        const uint32_t a = d.k * w.M + d.j;
+        const uint32_t q0 = lane * 2048u;
+        if (q0 < d.len)
+          bulk_g2s(smem_u32(tb + q0), src + (size_t)a * kWE + q0,
+                   min(2048u, d.len - q0) * (uint32_t)sizeof(Elem), full);
+      } else {
+        // the bucket's piece in every tile of the chunk: start, length, offset in the bucket
+        const uint32_t mk = chunk_tiles(d.k);
+        uint32_t p0[8], c[8], sum = 0;
 #pragma unroll
-      for (int q = 0; q < kWK; q++) {
-        const uint32_t pos = warp * 32u * kWK + (uint32_t)q * 32u + lane;
-        if (full || pos < len) v[q] = load_elem_stream(p + q * 32);
-      }
+        for (int r = 0; r < 8; r++) {
+          const uint32_t t = lane * 8u + r;
+          p0[r] = c[r] = 0;
+          if (t < mk) {
+            const uint16_t* pt = w.PT + ((size_t)s * w.M + t) * kPTS;
+            p0[r] = ld_relaxed_u16(pt + d.h);
+            c[r] = ld_relaxed_u16(pt + d.h + 1u) - p0[r];
+          }
+          sum += c[r];
+        }
+        uint32_t x = sum;
 #pragma unroll
-      for (int q = 0; q < kWK; q++) {
-        const uint32_t pos = warp * 32u * kWK + (uint32_t)q * 32u + lane;
-        dg[q] = (full || pos < len) ? digit_of(v[q].key, shift + 8, 0xFFu) : kSent;
+        for (int o = 1; o < 32; o <<= 1) {
+          const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+          if (lane >= (uint32_t)o) x += y;
+        }
+        uint32_t off = x - sum;
+        const uint32_t lo = d.i * kWE;
+#pragma unroll
+        for (int r = 0; r < 8; r++) {
+          const uint32_t t = lane * 8u + r;
+          const uint32_t a0 = max(off, lo), a1 = min(off + c[r], lo + d.len);
+          if (a0 < a1)
+            bulk_g2s(smem_u32(tb + (a0 - lo)), w.Z + (size_t)s * C + (size_t)t * kWE + p0[r] + (a0 - off),
+                     (a1 - a0) * (uint32_t)sizeof(Elem), full);
+          off += c[r];
+        }
+#pragma unroll
+        for (int r = 0; r < 8; r++) {
+          pre[b * 256u + lane + 32u * r] = nx_pre[lane + 32u * r];
+          gst[b * 256u + lane + 32u * r] = nx_gst[lane + 32u * r];
+        }
       }
-      if (full) rank_tile<true>(dg, r, wcnt, tcount, tstart, s_wt);
-      else rank_tile<false>(dg, r, wcnt, tcount, tstart, s_wt);
-      stage_tile(v, dg, r, wcnt, buf);
-      uint16_t* pt = w.PT + ((size_t)s * w.M + t) * kPTS;
-      if (tid < 256u) {
-        pt[tid] = (uint16_t)tstart[tid];
-        if (tcount[tid]) atomicAdd(&w.S[(size_t)k * 256u + tid], tcount[tid]);
-      } else if (tid == 256u) {
-        pt[256] = (uint16_t)len;
-      }
-      __syncthreads();
-      flush();  // the previous A tile (its copies have had this whole tile to drain)
-      if (tid < 4u && !error_raised(ctrl)) {
-        const uint32_t off = tid * (kWE / 4u);
-        if (off < len) {
-          fence_proxy_async_global();
-          bulk_s2g(w.Z + (size_t)s * C + (size_t)t * kWE + off, smem_u32(buf + off),
-                   min(kWE / 4u, len - off) * (uint32_t)sizeof(Elem));
+      if (lane == 0) s_desc[b] = d;
+      __syncwarp();
+      if (lane == 0) mbar_arrive(full);  // the description (and prefetches) are in place
+    };
+
+    // stores of the item staged in buffer b
+    auto issue_store = [&](uint32_t b) {
+      const ItemDesc d = s_desc[b];
+      Elem* tb = bufs + (size_t)b * kWE;
+      if (!error_raised(ctrl)) {
+        if (d.kind == kItemA) {
+          const uint32_t q0 = lane * 2048u;
+          if (q0 < d.len) {
+            fence_proxy_async_global();
+            bulk_s2g(w.Z + (size_t)(d.k % w.NZ) * C + (size_t)d.j * kWE + q0, smem_u32(tb + q0),
+                     min(2048u, d.len - q0) * (uint32_t)sizeof(Elem));
+          }
+        } else {
+#pragma unroll
+          for (int r = 0; r < 8; r++) {
+            const uint32_t l = lane + 32u * r;
+            const uint32_t cnt = tcount[b * 256u + l];
+            if (cnt) {
+              const uint32_t g = gbase[b * 256u + l];
+              if ((uint64_t)g + cnt > n) record_error(ctrl, kStatusInconsistent, kWhereScatter);
+              else bulk_s2g(dst + g, smem_u32(tb + tstart[b * 256u + l]), cnt * (uint32_t)sizeof(Elem));
+            }
+          }
         }
       }
       bulk_commit();
-      pending = (int32_t)k;
-      continue;
-    }
+      // the group before this one is complete: its A tile can be signalled
+      bulk_wait_one();
+      __syncwarp();
+      if (pend_a_old >= 0) signal_a((uint32_t)pend_a_old);
+      pend_a_old = pend_a;
+      pend_a = d.kind == kItemA ? (int32_t)d.k : -1;
+    };
 
-    // ---- B: one tile of bucket h of chunk k
-    const uint32_t k = s_k, j = s_j, s = k % w.NZ;
-    if (tid < 256u) {
-      const uint32_t f0 = ld_relaxed_u32(&w.first[s * kFirstStride + tid]);
-      const uint32_t f1 = ld_relaxed_u32(&w.first[s * kFirstStride + tid + 1u]);
-      if (f0 <= j && j < f1) {
-        s_h = tid;
-        s_i = j - f0;
-        s_J = f1 - f0;
+    while (!failed) {
+      bool progress = false;
+      // 1. store every tile the compute warps have staged
+      while (it_store < it_load &&
+             mbar_test_wait(smem_u32(&s_staged[it_store & 1u]), (it_store >> 1) & 1u)) {
+        issue_store(it_store & 1u);
+        it_store++;
+        progress = true;
       }
-    }
-    __syncthreads();
-    const uint32_t h = s_h, i = s_i, J = s_J;
-    const uint32_t Sh = ld_relaxed_u32(&w.S[(size_t)k * 256u + h]);
-    const uint32_t lo = i * kWE, len = min(kWE, Sh - lo);
-    const bool full = len == kWE;
-    const uint32_t mk = chunk_tiles(k);
-    // the bucket's piece in each tile of the chunk, and its offset in the bucket
-    uint32_t c = 0, p0 = 0;
-    if (tid < mk) {
-      const uint16_t* pt = w.PT + ((size_t)s * w.M + tid) * kPTS;
-      p0 = ld_relaxed_u16(pt + h);
-      c = ld_relaxed_u16(pt + h + 1u) - p0;
-    }
-    uint32_t tot;
-    const uint32_t off = block_exclusive_scan(c, s_wt, &tot);
-    fence_proxy_async_smem();  // this CTA's generic accesses of the buffer before the copies
-    if (tid == 0) mbar_arrive_expect_tx(bar, len * (uint32_t)sizeof(Elem));
-    __syncthreads();
-    if (tid < mk && c) {
-      const uint32_t a0 = max(off, lo), a1 = min(off + c, lo + len);
-      if (a0 < a1) {
-        fence_proxy_async_global();
-        bulk_g2s(smem_u32(buf + (a0 - lo)),
-                 w.Z + (size_t)s * C + (size_t)tid * kWE + p0 + (a0 - off),
-                 (a1 - a0) * (uint32_t)sizeof(Elem), bar);
+      if (done && it_store == it_load) break;
+      // 2. choose the next item
+      if (!done && !have_nx) {
+        uint32_t kind = kNone;
+        if (lane == 0) {
+          kind = try_pick(nx);
+          if (kind == kDone) nx.kind = kDone;
+        }
+        kind = __shfl_sync(0xffffffffu, kind, 0);
+        if (kind != kNone) {
+          nx.kind = __shfl_sync(0xffffffffu, nx.kind, 0);
+          nx.k = __shfl_sync(0xffffffffu, nx.k, 0);
+          nx.j = __shfl_sync(0xffffffffu, nx.j, 0);
+          nx.len = __shfl_sync(0xffffffffu, nx.len, 0);
+          have_nx = true;
+          nx_pre_ok = nx.kind != kItemB;
+          progress = true;
+        }
+        pmark(4);
       }
+      // 3. a B tile's bucket prefix (may have to wait for an earlier chunk)
+      if (have_nx && !nx_pre_ok) {
+        const long long e0 = clock64();
+        nx_pre_ok = prepare_b(nx);
+        if (prof && lane == 0) s_prof[5] += (unsigned long long)(clock64() - e0);
+        if (nx_pre_ok) progress = true;
+      }
+      // 4. load it once its buffer is free (the item two back has been stored and read out)
+      if (have_nx && nx_pre_ok && it_load < it_store + 2u) {
+        const uint32_t b = it_load & 1u;
+        if (it_load >= 2u) {
+          // the stores of item it_load - 2 (the newest or the second newest group) must have read the buffer
+          if (it_store - 1u == it_load - 2u) bulk_wait_read_all();
+          else bulk_wait_read_one();
+          __syncwarp();
+        }
+        if (nx.kind == kDone) {
+          // no more work: tell the compute warps (the marker is not an item)
+          if (lane == 0) {
+            s_desc[b].kind = kDone;
+            mbar_arrive(smem_u32(&s_full[b]));
+            mbar_arrive(smem_u32(&s_full[b]));
+          }
+          __syncwarp();
+          done = true;
+        } else {
+          issue_load(nx, b);
+          if (prof && lane == 0) s_prof[nx.kind == kItemA ? 7 : 8] += 1ull;
+          it_load++;
+        }
+        have_nx = false;
+        progress = true;
+      }
+      if (progress) {
+        idle = 0;
+        ns = 8;
+        continue;
+      }
+      // nothing to do: complete this CTA's pending A tiles first (their chunk
+      // plans may be what everybody waits for), then back off
+      if (pend_a >= 0 || pend_a_old >= 0) {
+        drain();
+        continue;
+      }
+      if (lane == 0 && prof) s_prof[9] += 1ull;
+      if (++idle >= kSpinLimit || ((idle & 63u) == 0u && error_raised(ctrl))) {
+        if (lane == 0 && !error_raised(ctrl)) record_error(ctrl, kStatusTimeout, kWhereSchedule);
+        failed = true;
+        break;
+      }
+      __nanosleep(ns);
+      if (ns < 256) ns <<= 1;
     }
-    const bool arrived = mbar_wait_bounded(bar, phase);
-    if (__syncthreads_or(!arrived)) {
+    // (after a failure the compute warps' own bounded waits end them)
+    __syncwarp();
+    drain();
+    if (prof && lane == 0) {
+      s_prof[10] = (unsigned long long)(clock64() - t_start);
+      for (int f = 4; f < 12; f++) atomicAdd(&ctrl->wide_prof[pass][f], s_prof[f]);
+    }
+    return;
+  }
+
+  // =================== compute warps ===================
+  long long t_mark = clock64();
+  auto cmark = [&](int f) {
+    if (prof && tid == 0) {
+      const long long now = clock64();
+      s_prof[f] += (unsigned long long)(now - t_mark);
+      t_mark = now;
+    }
+  };
+  for (uint32_t it = 0;; it++) {
+    const uint32_t b = it & 1u;
+    const bool arrived = mbar_wait_bounded(smem_u32(&s_full[b]), (it >> 1) & 1u);
+    if (compute_sync_or(!arrived)) {
       record_error(ctrl, kStatusTimeout, kWhereBulkCopy);
-      gather_pending = true;
       break;
     }
-    phase ^= 1u;
+    cmark(0);
+    const ItemDesc d = s_desc[b];
+    if (d.kind == kDone) break;
+    Elem* tb = bufs + (size_t)b * kWE;
+    uint32_t* tc = tcount + b * 256u;
+    uint32_t* ts = tstart + b * 256u;
+    const bool full = d.len == kWE;
+    const int dshift = d.kind == kItemA ? shift + 8 : shift;
+    Elem v[kWK];
+    uint32_t r[kWK];
 #pragma unroll
     for (int q = 0; q < kWK; q++) {
       const uint32_t pos = warp * 32u * kWK + (uint32_t)q * 32u + lane;
-      if (full || pos < len) {
-        v[q] = lds_elem(buf + pos);
-        dg[q] = digit_of(v[q].key, shift, 0xFFu);
-      } else {
-        dg[q] = kSent;
-      }
+      if (full || pos < d.len) v[q] = lds_elem(tb + pos);
+      else v[q].key = v[q].val = 0;
     }
-    if (full) rank_tile<true>(dg, r, wcnt, tcount, tstart, s_wt);
-    else rank_tile<false>(dg, r, wcnt, tcount, tstart, s_wt);
-
-    // elements of digit (h, tid) before this tile: earlier chunks (R) plus
-    // earlier tiles of this bucket in this chunk (look-back)
-    const uint32_t tag = wide_tag(pass, k, j);
-    uint64_t* ring = w.status + (size_t)s * w.nbmax * 256u;
-    uint64_t* my = ring + (size_t)j * 256u;
-    uint32_t excl = 0;
+    if (full) rank_tile<true>(v, dshift, d.len, r, wcnt, tc, ts, s_wt);
+    else rank_tile<false>(v, dshift, d.len, r, wcnt, tc, ts, s_wt);
     bool timed_out = false;
-    if (i == 0) {
-      if (tid == 0) {
-        // the last earlier chunk with elements in bucket h must have folded its counts
-        int32_t kp = (int32_t)k - 1;
-        while (kp >= 0 && ld_relaxed_u32(&w.S[(size_t)kp * 256u + h]) == 0u) kp--;
-        if (kp >= 0) timed_out = wait_bucket_epoch(&w.epoch[h], (uint32_t)kp + 1u, ctrl);
-      }
-      __syncthreads();
+    if (d.kind == kItemA) {
+      // piece table row and bucket sizes of the chunk
+      const uint32_t s = d.k % w.NZ;
+      uint16_t* pt = w.PT + ((size_t)s * w.M + d.j) * kPTS;
       if (tid < 256u) {
-        excl = ld_relaxed_u32(&w.R[h * 256u + tid]);
-        if (J > 1u) {
-          // the bucket's last tile overwrites R once its walk has seen this
-          // status: the read of R above must be ordered before it
+        pt[tid] = (uint16_t)ts[tid];
+        if (tc[tid]) atomicAdd(&w.S[(size_t)d.k * 256u + tid], tc[tid]);
+      } else if (tid == 256u) {
+        pt[256] = (uint16_t)d.len;
+      }
+    } else {
+      // elements of digit (h, tid) before this tile: the running prefix of
+      // earlier chunks (prefetched) plus earlier tiles of the bucket (look-back)
+      const uint32_t s = d.k % w.NZ;
+      const uint32_t tag = wide_tag(pass, d.k, d.j);
+      uint64_t* ring = w.status + (size_t)s * w.nbmax * 256u;
+      uint64_t* my = ring + (size_t)d.j * 256u;
+      uint32_t excl = 0;
+      if (tid < 256u) {
+        if (d.i == 0) {
+          excl = pre[b * 256u + tid];
+          if (d.J > 1u) {
+            // the bucket's last tile overwrites R once its walk has seen this
+            // status: the read of R must be ordered before it
+            __threadfence();
+            st_relaxed_u64(my + tid, pack_status(kFlagIncl, tag, excl + tc[tid]));
+          }
+        } else {
+          st_relaxed_u64(my + tid, pack_status(kFlagAgg, tag, tc[tid]));
+          timed_out = walk_bucket(ring, d.j, tid, pass, d.k, ctrl, &excl);
+          st_relaxed_u64(my + tid, pack_status(kFlagIncl, tag, excl + tc[tid]));
+        }
+        gbase[b * 256u + tid] = gst[b * 256u + tid] + excl;
+      }
+      if (d.i + 1u == d.J) {
+        // the bucket's last tile: hand the running prefix on to the next chunk
+        __threadfence();
+        if (tid < 256u) st_relaxed_u32(&w.R[d.h * 256u + tid], excl + tc[tid]);
+        compute_sync();
+        if (tid == 0) {
           __threadfence();
-          st_relaxed_u64(my + tid, pack_status(kFlagIncl, tag, excl + tcount[tid]));
+          st_release_u32(&w.epoch[d.h], d.k + 1u);
         }
       }
-    } else if (tid < 256u) {
-      st_relaxed_u64(my + tid, pack_status(kFlagAgg, tag, tcount[tid]));
-      timed_out = walk_bucket(ring, j, tid, pass, k, ctrl, &excl);
-      st_relaxed_u64(my + tid, pack_status(kFlagIncl, tag, excl + tcount[tid]));
-    }
-    if (tid < 256u) gbase[tid] = gstart[(h << 8) | tid] + excl;
-    if (i + 1u == J) {
-      // the bucket's last tile: hand the running prefix on to the next chunk
-      __threadfence();
-      if (tid < 256u) st_relaxed_u32(&w.R[h * 256u + tid], excl + tcount[tid]);
-      __syncthreads();
+      if (compute_sync_or(timed_out)) break;
       if (tid == 0) {
         __threadfence();
-        st_release_u32(&w.epoch[h], k + 1u);
+        atomicAdd(&w.chunks[d.k].bdone, 1u);  // done with Z, the piece table and the ring slot
       }
     }
-    if (__syncthreads_or(timed_out)) break;
-    if (tid == 0) {
-      __threadfence();
-      atomicAdd(&w.chunks[k].bdone, 1u);  // done with Z, the piece table and the ring slot
-    }
-    stage_tile(v, dg, r, wcnt, buf);
-    __syncthreads();
-    flush();
-    if (tid < 256u && !error_raised(ctrl)) {
-      const uint32_t cnt = tcount[tid];
-      if (cnt) {
-        const uint32_t g = gbase[tid];
-        if ((uint64_t)g + cnt > n) record_error(ctrl, kStatusInconsistent, kWhereScatter);
-        else bulk_s2g(dst + g, smem_u32(buf + tstart[tid]), cnt * (uint32_t)sizeof(Elem));
-      }
-    }
-    bulk_commit();
+    compute_sync();  // every item of the tile is in registers: the buffer is free for staging
+#pragma unroll
+    for (int q = 0; q < kWK; q++)
+      if (full || warp * 32u * kWK + (uint32_t)q * 32u + lane < d.len)
+        tb[r[q] + wcnt[digit_of(v[q].key, dshift, 0xFFu) * kWWP + warp]] = v[q];
+    fence_proxy_async_smem();
+    __syncwarp();
+    for (uint32_t bin = lane; bin < 256u; bin += 32u) wcnt[bin * kWWP + warp] = 0u;
+    compute_sync();
+    if (tid == 0) mbar_arrive(smem_u32(&s_staged[b]));
+    cmark(d.kind == kItemA ? 1 : 2);
   }
-  flush();
-  // leaving after an error: copies still landing in shared memory must finish first
-  if (gather_pending) mbar_wait_bounded(bar, phase);
-  bulk_wait_all();
+  if (prof && tid == 0) {
+    for (int f = 0; f < 4; f++) atomicAdd(&ctrl->wide_prof[pass][f], s_prof[f]);
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -695,7 +1168,7 @@ size_t wide_layout_bytes(uint32_t n, size_t* pass_zero_bytes, size_t* ring_bytes
 }
 
 static size_t wide_smem() {
-  return (size_t)kWE * sizeof(Elem) + 256u * kWWP * 4u + 3u * 256u * 4u;
+  return 2u * (size_t)kWE * sizeof(Elem) + 256u * kWWP * 4u + 5u * 512u * 4u + 2u * 256u * 4u;
 }
 
 int wide_run(Elem* X, Elem* Y, int first_digit, int target_parity, unsigned char* ws,
@@ -706,11 +1179,11 @@ int wide_run(Elem* X, Elem* Y, int first_digit, int target_parity, unsigned char
   unsigned char* wbase = ws + L.off_wide;
   DeviceInfo dev;
   if (int rc = current_device_info(&dev)) return rc;
-  if (int rc = hist16(X, L.n, first_digit, L.num_digits, hist, st)) return rc;
+  if (int rc = hist16(X, L.n, first_digit, L.num_digits, hist, st, ctrl)) return rc;
   {
     ProfScope prof("plan", st);
-    k_plan<<<1, 1024, 0, st>>>(hist, gstart, L.n, 16, L.num_digits, target_parity, L.api_bits,
-                               L.sub, ctrl);
+    k_plan16_scan<<<L.num_digits, kPlan16Threads, 0, st>>>(hist, gstart, L.n, ctrl);
+    k_plan16_parity<<<1, 32, 0, st>>>(L.num_digits, target_parity, L.api_bits, L.n, ctrl);
   }
   if (cudaPeekAtLastError() != cudaSuccess) return 5;
   size_t zero_bytes = 0, ring_bytes = 0, offs[9];
@@ -726,6 +1199,7 @@ int wide_run(Elem* X, Elem* Y, int first_digit, int target_parity, unsigned char
   a.PT = reinterpret_cast<uint16_t*>(wbase + offs[7]);
   a.Z = reinterpret_cast<Elem*>(wbase + offs[8]);
   wide_geometry(L.n, &a.M, &a.NZ, &a.K, &a.nbmax, &a.totalA);
+  a.prof = std::getenv("LSB_WIDE_PROFILE") != nullptr;
   if (cudaMemsetAsync(a.status, 0, ring_bytes, st) != cudaSuccess) return 5;
   const size_t smem = wide_smem();
   if (cudaFuncSetAttribute(k_wide, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
@@ -792,6 +1266,7 @@ int selftest_wide_wait(int which, unsigned char* ws, cudaStream_t st) {
   a.PT = reinterpret_cast<uint16_t*>(wbase + offs[7]);
   a.Z = reinterpret_cast<Elem*>(wbase + offs[8]);
   wide_geometry(kWE, &a.M, &a.NZ, &a.K, &a.nbmax, &a.totalA);
+  a.prof = 0;
   const uint32_t taken = a.totalA;  // every A tile already handed out
   if (cudaMemcpyAsync(&a.ctl->aticket, &taken, sizeof taken, cudaMemcpyHostToDevice, st) != cudaSuccess ||
       cudaStreamSynchronize(st) != cudaSuccess)

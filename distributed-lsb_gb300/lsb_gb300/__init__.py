@@ -81,7 +81,8 @@ class KernelTime(ctypes.Structure):
 class Tuning(ctypes.Structure):
     """lsb_tuning_t"""
 
-    _fields_ = [("digit_bits", ctypes.c_int32), ("variant", ctypes.c_int32), ("reserved", ctypes.c_int32 * 2)]
+    _fields_ = [("digit_bits", ctypes.c_int32), ("variant", ctypes.c_int32), ("ctas", ctypes.c_int32),
+                ("reserved", ctypes.c_int32)]
 
 
 class ServerConfig(ctypes.Structure):

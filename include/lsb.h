@@ -169,7 +169,8 @@ typedef struct lsb_tuning {
   int32_t digit_bits; /* digit width of the passes (result identical for all)  */
   int32_t variant;    /* kernel shape: 0 = 8192-element tiles, 1 CTA per SM;
                          2 = 4096-element tiles, 2 CTAs per SM                 */
-  int32_t reserved[2];
+  int32_t ctas;       /* persistent CTAs of the passes (0 = every resident slot) */
+  int32_t reserved;
 } lsb_tuning_t;
 
 /* Workspace for lsb_sort_segmented / lsb_graph_capture_segmented (any variant). */
@@ -183,8 +184,9 @@ int lsb_sort_segmented(lsb_elem_t* d_a, lsb_elem_t* d_b, int64_t n_total,
                        const int64_t* d_seg_offsets, int64_t nseg, const lsb_tuning_t* opt_tuning,
                        void* d_workspace, size_t workspace_bytes, void* stream);
 
-/* Autotuner: times every candidate configuration (digit width 8 or 11, kernel
- * shape 0 or 2) on a sample batch with the same segment sizes as
+/* Autotuner: times every candidate configuration (digit width 8, 11 or 16,
+ * kernel shape 0 or 2, all resident CTAs or one per SM or half the SMs) on a
+ * sample batch with the same segment sizes as
  * h_seg_offsets (host array, nseg + 1 entries; random keys, at most ~2^26
  * elements) and returns the fastest. Results are cached per size class (log2
  * of the total and of the mean segment size). Blocking; allocates. */

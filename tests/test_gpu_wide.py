@@ -12,7 +12,13 @@ from conftest import to_dev, to_np
 
 pytestmark = pytest.mark.gpu
 
-TILE = 8192  # elements per tile of the wide kernel
+TILE = 6144  # elements per tile of the wide kernel
+
+
+@pytest.fixture(autouse=True)
+def wide_family(monkeypatch):
+    """16-bit digits through the one-pass family in every test of this file."""
+    monkeypatch.setenv("LSB_WIDE_DIGITS", "wide")
 
 
 def _sort(lsb, torch, a, bits=16):
