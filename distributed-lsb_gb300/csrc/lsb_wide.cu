@@ -44,12 +44,13 @@
 
 namespace lsb {
 
-constexpr int kCW = 16;                  // compute warps per CTA
-constexpr uint32_t kCT = kCW * 32;       // compute threads
-constexpr int kWT = kCT + 32;            // + one producer warp
-constexpr int kWK = 12;                  // items per compute thread
-constexpr uint32_t kWE = kCT * kWK;      // elements per tile (A and B): 6144
-constexpr int kWWP = kCW + 1;            // padded counter row (distinct banks per lane)
+constexpr int kWT = 512;                 // threads per CTA
+constexpr int kWW = kWT / 32;            // warps per CTA
+constexpr int kWK = 16;                  // A tile: items per thread
+constexpr uint32_t kWE = kWT * kWK;      // A tile: 8192 elements
+constexpr int kWWP = kWW + 1;            // padded counter row (distinct banks per lane)
+constexpr uint32_t kBQ = 16384;          // B item: at most this many elements of one bucket
+constexpr int kBU = 4;                   // B item: elements per lane in flight
 constexpr uint32_t kPTS = 264;           // piece-table row: 257 u16 starts, padded to 16 B
 constexpr uint32_t kFirstStride = 264;   // per-slot B-tile numbering: 257 u32
 constexpr uint32_t kNone = 0, kItemA = 1, kItemB = 2, kDone = 3;
@@ -86,11 +87,10 @@ struct WideArgs {
 };
 
 // Phases of ctrl->wide_prof[pass][*] (diagnostics; thread 0 of every CTA).
-//   0  compute warps: cycles waiting for their next tile to be loaded
-//   1  compute warps: cycles in A tiles      2  compute warps: cycles in B tiles
-//   4  producer: cycles choosing work        5  producer: B prefix prefetch (incl. waits)
-//   7  A tiles loaded    8  B tiles loaded    9  producer polls that found nothing to do
-//  10  producer: cycles from kernel start to end
+//   1  cycles in A tiles          2  cycles in batches of B items
+//   4  cycles choosing work        7  A tiles        8  B items
+//   9  polls that found nothing to do   10  cycles from kernel start to end
+//  11  cycles signalling A tiles' completion (and building chunk plans)
 
 __device__ __forceinline__ uint32_t ld_relaxed_u16(const uint16_t* p) {
   unsigned short v;
@@ -497,96 +497,23 @@ __global__ void k_plan16_parity(int num_digits, int target_parity, int api_bits,
 }
 
 // ---------------------------------------------------------------------------
-// the pass: one producer warp (choice of work, bulk-copy loads and gathers
-// into shared memory, prefetch of each bucket's running prefix and digit
-// starts, the stores) and kCW compute warps (ranking and staging), over two
-// tile buffers in shared memory, so that a tile's memory traffic overlaps the
-// ranking of the tile before it
-
-// Per-buffer description of the tile it holds, written by the producer
-// before it releases the buffer's full barrier.
-struct ItemDesc {
-  uint32_t kind;     // kItemA, kItemB or kDone
-  uint32_t k, j;     // chunk; A: tile of the chunk, B: B tile of the chunk
-  uint32_t len;      // elements in the tile
-  uint32_t h, i, J;  // B: bucket, tile of the bucket, tiles of the bucket
-  uint32_t pad;
-};
-
-__device__ __forceinline__ void compute_sync() {
-  asm volatile("bar.sync 1, %0;" ::"n"(kCT) : "memory");
-}
-// barrier of the compute warps that returns whether any of them passed `p`
-__device__ __forceinline__ bool compute_sync_or(bool p) {
-  uint32_t r;
-  asm volatile(
-      "{\n .reg .pred a, b;\n setp.ne.u32 a, %1, 0;\n barrier.red.or.pred b, 1, %2, a;\n"
-      " selp.u32 %0, 1, 0, b;\n}\n"
-      : "=r"(r)
-      : "r"((uint32_t)p), "n"(kCT)
-      : "memory");
-  return r != 0;
-}
-// exclusive scan of one value per compute thread (compute warps only)
-__device__ __forceinline__ uint32_t compute_exclusive_scan(uint32_t v, uint32_t* warp_tot,
-                                                           uint32_t* total) {
-  const uint32_t lane = lane_id(), warp = threadIdx.x >> 5;
-  uint32_t x = v;
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
-    if (lane >= (uint32_t)o) x += y;
-  }
-  if (lane == 31) warp_tot[warp] = x;
-  compute_sync();
-  if (warp == 0) {
-    const uint32_t t = lane < (uint32_t)kCW ? warp_tot[lane] : 0u;
-    uint32_t s = t;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const uint32_t y = __shfl_up_sync(0xffffffffu, s, o);
-      if (lane >= (uint32_t)o) s += y;
-    }
-    if (lane < (uint32_t)kCW) warp_tot[lane] = s - t;
-    if (lane == (uint32_t)kCW - 1) warp_tot[32] = s;
-  }
-  compute_sync();
-  const uint32_t r = warp_tot[warp] + x - v;
-  *total = warp_tot[32];
-  compute_sync();
-  return r;
-}
-__device__ __forceinline__ bool mbar_test_wait(uint32_t bar, uint32_t phase) {
-  uint32_t ok;
-  asm volatile(
-      "{\n .reg .pred p;\n mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n"
-      " selp.u32 %0, 1, 0, p;\n}\n"
-      : "=r"(ok)
-      : "r"(bar), "r"(phase)
-      : "memory");
-  return ok != 0;
-}
-__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
-  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
-}
-__device__ __forceinline__ void bulk_wait_read_one() {
-  asm volatile("cp.async.bulk.wait_group.read 1;" ::: "memory");
-}
-__device__ __forceinline__ void bulk_wait_one() {
-  asm volatile("cp.async.bulk.wait_group 1;" ::: "memory");
-}
+// the pass: A tiles by whole CTAs (rank by the high byte, stage, one bulk
+// copy into the chunk buffer), B items by single warps (one bucket of one
+// chunk: its pieces read from the chunk buffer in input order, ranked by the
+// low byte with warp ballots and per-warp counters, each element stored
+// straight to its final position). A CTA takes either one A tile or up to one
+// B item per warp.
 
 // Stable rank of each item's 8-bit digit inside its warp (peers from ballots,
-// per-warp counters [256][kWWP], zero on entry), then the tile's per-digit
+// per-warp counters [256][kWWP], zero on entry); then the tile's per-digit
 // totals (tcount), tile-local starts (tstart) and per-(digit, warp) starts
-// written back into the counters. Items with dg == kSent are not counted.
-// Compute warps only.
+// written back into the counters. Items at or past `len` are not counted.
 // The digit of item q is (v[q].key >> dshift) & 0xff, recomputed where it is
-// needed rather than kept in registers; item q of lane l in warp w is tile
-// position w*32*kWK + q*32 + l, valid below len.
+// needed; item q of lane l in warp w is tile position w*32*kWK + q*32 + l.
+// Ranks are below 2^16: r2[q / 2] holds those of items q (low half) and q + 1.
 template <bool FULL>
 __device__ __forceinline__ void rank_tile(const Elem (&v)[kWK], int dshift, uint32_t len,
-                                          uint32_t (&r)[kWK], uint32_t* wcnt, uint32_t* tcount,
+                                          uint32_t (&r2)[kWK / 2], uint32_t* wcnt, uint32_t* tcount,
                                           uint32_t* tstart, uint32_t* s_wt) {
   const uint32_t warp = threadIdx.x >> 5, lt = lanemask_lt();
   const uint32_t base = warp * 32u * kWK + lane_id();
@@ -597,57 +524,86 @@ __device__ __forceinline__ void rank_tile(const Elem (&v)[kWK], int dshift, uint
     const uint32_t peers = FULL ? warp_peers_fixed<8>(dg) : warp_peers(dg, 8, valid);
     uint32_t c = 0;
     if (valid) c = wcnt[dg * kWWP + warp];
-    r[q] = c + __popc(peers & lt);
+    const uint32_t rk = c + __popc(peers & lt);
+    if (q & 1) r2[q / 2] |= rk << 16;
+    else r2[q / 2] = rk;
     __syncwarp();
     if (valid) wcnt[dg * kWWP + warp] = c + __popc(peers);  // every peer writes the same count
     __syncwarp();
   }
-  compute_sync();
+  __syncthreads();
   const uint32_t b = threadIdx.x;
   uint32_t sum = 0;
   if (b < 256u) {
 #pragma unroll
-    for (int w = 0; w < kCW; w++) sum += wcnt[b * kWWP + w];
+    for (int w = 0; w < kWW; w++) sum += wcnt[b * kWWP + w];
     tcount[b] = sum;
   }
   uint32_t tot;
-  uint32_t off = compute_exclusive_scan(sum, s_wt, &tot);
+  uint32_t off = block_exclusive_scan(sum, s_wt, &tot);
   if (b < 256u) {
     tstart[b] = off;
 #pragma unroll
-    for (int w = 0; w < kCW; w++) {
+    for (int w = 0; w < kWW; w++) {
       const uint32_t c = wcnt[b * kWWP + w];
       wcnt[b * kWWP + w] = off;
       off += c;
     }
   }
-  compute_sync();
+  __syncthreads();
 }
 
-// 17 warps: the register file is split over the SM's four schedulers, so
-// one of them holds five warps and the kernel gets at most 96 registers per
-// thread.
+// 16-byte load through L2 only: chunk buffers are rewritten from chunk to
+// chunk, so an L1 copy could be stale
+__device__ __forceinline__ Elem load_elem_cg(const Elem* p) {
+  Elem e;
+  asm volatile("ld.global.cg.v2.u64 {%0, %1}, [%2];" : "=l"(e.key), "=l"(e.val) : "l"(p) : "memory");
+  return e;
+}
+
+// Per-warp shared state of a B item.
+struct BWarp {
+  uint32_t cnt[256];     // elements of each low byte placed so far (or counted)
+  uint32_t gbase[256];   // destination of the item's first element of each low byte
+  uint32_t poff[257];    // offset of each tile's piece in the bucket; poff[mk] = bucket size
+  uint32_t psrc[256];    // Z index (in the chunk slot) of each tile's piece
+};
+
+// First piece whose range holds bucket position `pos` (poff ascending).
+__device__ __forceinline__ uint32_t first_piece(const uint32_t* poff, uint32_t mk, uint32_t pos) {
+  uint32_t a0 = 0, a1 = mk;
+  while (a0 + 1u < a1) {
+    const uint32_t m = (a0 + a1) >> 1;
+    if (poff[m] <= pos) a0 = m;
+    else a1 = m;
+  }
+  return a0;
+}
+
 __global__ void __launch_bounds__(kWT, 1)
     k_wide(Elem* __restrict__ X, Elem* __restrict__ Y, uint32_t n, int pass, int digit,
            const uint32_t* __restrict__ gstart, WideArgs w, Ctrl* ctrl) {
   constexpr uint32_t kSent = 0xffffffffu;
   extern __shared__ __align__(16) unsigned char smem[];
-  __shared__ __align__(8) uint64_t s_full[2], s_staged[2];
-  __shared__ ItemDesc s_desc[2];
   __shared__ uint32_t s_wt[33];
-  __shared__ uint32_t s_first[260], s_size[256];  // producer: plan of its current B chunk
+  __shared__ uint32_t s_kind, s_a, s_k, s_j0, s_nj, s_flag;
+  __shared__ uint32_t s_first[264], s_size[256];  // plan of the CTA's current B chunk
+  __shared__ uint32_t s_plan_k;
   __shared__ unsigned long long s_prof[12];
+  // scheduler state of thread 0, kept in shared memory (the registers are the
+  // A tile's): an A tile taken whose Z slot was not free yet; the current B
+  // chunk, whether its plan is known and its B item count; idle back-off
+  __shared__ uint32_t s_held_a, s_cb_k, s_cb_nb, s_cb_ready, s_idle, s_ns;
+  __shared__ int32_t s_pending;  // chunk of this CTA's last A tile, completion not yet signalled
+  __shared__ long long s_t_mark, s_t_start;
 
   if (pass_skipped(ctrl, pass)) return;
-  Elem* bufs = reinterpret_cast<Elem*>(smem);                                       // [2][kWE]
-  uint32_t* wcnt = reinterpret_cast<uint32_t*>(smem + 2u * kWE * sizeof(Elem));     // [256][kWWP]
-  uint32_t* tcount = wcnt + 256 * kWWP;  // [2][256] per-digit counts of the tile in each buffer
-  uint32_t* tstart = tcount + 512;       // [2][256] tile-local start of each digit
-  uint32_t* gbase = tstart + 512;        // [2][256] B: destination of each digit's run
-  uint32_t* pre = gbase + 512;           // [2][256] B: running prefix R[h][l] (first tile of a bucket)
-  uint32_t* gst = pre + 512;             // [2][256] B: digit starts start(h, l)
-  uint32_t* nx_pre = gst + 512;          // [256] producer: R[h][l] of the next B tile, staged
-  uint32_t* nx_gst = nx_pre + 256;       // [256] producer: start(h, l) of the next B tile, staged
+  // the A tile's staging buffer and the warps' B state share the same bytes
+  Elem* buf = reinterpret_cast<Elem*>(smem);                                        // [kWE]
+  BWarp* bw = reinterpret_cast<BWarp*>(smem);                                       // [kWW]
+  uint32_t* wcnt = reinterpret_cast<uint32_t*>(smem + (size_t)kWE * sizeof(Elem));  // [256][kWWP]
+  uint32_t* tcount = wcnt + 256 * kWWP;                                             // [256]
+  uint32_t* tstart = tcount + 256;                                                  // [256]
 
   const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = lane_id();
   const uint32_t par = ctrl->parity[pass];
@@ -660,462 +616,372 @@ __global__ void __launch_bounds__(kWT, 1)
   for (uint32_t i = tid; i < 256u * kWWP; i += kWT) wcnt[i] = 0u;
   if (tid < 12u) s_prof[tid] = 0ull;
   if (tid == 0) {
-    for (int b = 0; b < 2; b++) {
-      mbar_init(smem_u32(&s_full[b]), 2);    // the producer's two arrivals (+ copied bytes)
-      mbar_init(smem_u32(&s_staged[b]), 1);  // compute thread 0
-    }
-    fence_mbar_init();
+    s_plan_k = kSent;
+    s_held_a = kSent;
+    s_cb_k = s_cb_nb = s_cb_ready = s_idle = 0;
+    s_ns = 8;
+    s_pending = -1;
+    s_t_mark = s_t_start = clock64();
   }
   __syncthreads();
-  const long long t_start = clock64();
+  auto mark = [&](int f) {
+    if (prof && tid == 0) {
+      const long long now = clock64();
+      s_prof[f] += (unsigned long long)(now - s_t_mark);
+      s_t_mark = now;
+    }
+  };
 
-  if (warp == (uint32_t)kCW) {
-    // =================== producer warp ===================
-    uint32_t held_a = kSent;               // lane 0: A tile taken whose Z slot was not free yet
-    uint32_t cb_k = 0, cb_nb = 0;          // lane 0: current B chunk and its B tile count
-    bool cb_ready = false;
-    uint32_t plan_k = kSent;               // chunk whose plan is in s_first / s_size
-    uint32_t it_load = 0, it_store = 0;    // next item to load / to store
-    int32_t pend_a = -1;                   // chunk of an A tile whose stores are in the
-                                           // newest bulk group, signalled once complete
-    int32_t pend_a_old = -1;               // the same for the group before it
-    bool done = false, failed = false;
-    uint32_t idle = 0, ns = 8;
-    // the item chosen for loading (uniform across the warp)
-    ItemDesc nx;
-    bool have_nx = false, nx_pre_ok = false;
-    long long t_mark = clock64();
-    auto pmark = [&](int f) {
-      if (prof && lane == 0) {
-        const long long now = clock64();
-        s_prof[f] += (unsigned long long)(now - t_mark);
-        t_mark = now;
-      }
-    };
+  auto chunk_tiles = [&](uint32_t k) { return min(w.M, w.totalA - k * w.M); };
 
-    auto chunk_tiles = [&](uint32_t k) { return min(w.M, w.totalA - k * w.M); };
+  // B item numbering of chunk k, once all its A tiles are done: bucket h gets
+  // ceil(S[k][h] / kBQ) items (none when empty). CTA-wide.
+  auto build_plan = [&](uint32_t k) {
+    const uint32_t s = k % w.NZ;
+    if (tid == 0) __threadfence();  // acquire: the other A tiles' bucket counts
+    __syncthreads();
+    uint32_t J = 0;
+    if (tid < 256u) J = (ld_relaxed_u32(&w.S[(size_t)k * 256u + tid]) + kBQ - 1u) / kBQ;
+    uint32_t tot;
+    const uint32_t ex = block_exclusive_scan(J, s_wt, &tot);
+    if (tid < 256u) st_relaxed_u32(&w.first[s * kFirstStride + tid], ex);
+    if (tid == 0) {
+      st_relaxed_u32(&w.first[s * kFirstStride + 256u], tot);
+      st_relaxed_u32(&w.chunks[k].nb, tot);
+    }
+    __syncthreads();
+    if (tid == 0) {
+      __threadfence();
+      st_release_u32(&w.chunks[k].plan_ready, 1u);
+    }
+  };
 
-    // Signals that a chunk's A tile is complete in Z (its stores finished);
-    // the chunk's last one also publishes the chunk's plan.
-    auto signal_a = [&](uint32_t k) {
+  // Signals that this CTA's last A tile is complete in Z (its bulk copy is
+  // done). CTA-wide; builds the chunk's plan if that tile was its last one.
+  auto flush = [&]() {
+    const int32_t pend = s_pending;  // uniform: written by thread 0 before a barrier
+    if (pend < 0) return;
+    if (tid == 0) {
+      bulk_wait_all();
       fence_proxy_async_global();
       __threadfence();
-      __syncwarp();
-      uint32_t last = 0;
-      if (lane == 0) last = atomicAdd(&w.chunks[k].adone, 1u) + 1u == chunk_tiles(k) ? 1u : 0u;
-      last = __shfl_sync(0xffffffffu, last, 0);
-      if (!last) return;
-      __threadfence();  // acquire: the other A tiles' bucket counts
-      const uint32_t s = k % w.NZ;
-      uint32_t Jl[8], sum = 0;
-#pragma unroll
-      for (int r = 0; r < 8; r++) {
-        Jl[r] = (ld_relaxed_u32(&w.S[(size_t)k * 256u + lane * 8u + r]) + kWE - 1u) / kWE;
-        sum += Jl[r];
-      }
-      uint32_t x = sum;
-#pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
-        if (lane >= (uint32_t)o) x += y;
-      }
-      uint32_t ex = x - sum;
-#pragma unroll
-      for (int r = 0; r < 8; r++) {
-        st_relaxed_u32(&w.first[s * kFirstStride + lane * 8u + r], ex);
-        ex += Jl[r];
-      }
-      if (lane == 31) {
-        st_relaxed_u32(&w.first[s * kFirstStride + 256u], x);
-        st_relaxed_u32(&w.chunks[k].nb, x);
-      }
-      __threadfence();
-      __syncwarp();
-      if (lane == 0) st_release_u32(&w.chunks[k].plan_ready, 1u);
-    };
-    // all bulk groups complete: signal every pending A tile
-    auto drain = [&]() {
-      bulk_wait_all();
-      __syncwarp();
-      if (pend_a_old >= 0) signal_a((uint32_t)pend_a_old);
-      if (pend_a >= 0) signal_a((uint32_t)pend_a);
-      pend_a = pend_a_old = -1;
-    };
+      s_flag = atomicAdd(&w.chunks[pend].adone, 1u) + 1u == chunk_tiles((uint32_t)pend) ? 1u : 0u;
+    }
+    __syncthreads();
+    if (s_flag) build_plan((uint32_t)pend);
+    if (tid == 0) s_pending = -1;
+    __syncthreads();
+    mark(11);
+  };
 
-    // lane 0: the next item, without waiting (kNone if nothing is runnable now)
-    auto try_pick = [&](ItemDesc& d) -> uint32_t {
-      if (error_raised(ctrl)) return kDone;
-      for (;;) {
-        if (cb_k >= w.K) break;
-        if (!cb_ready) {
-          if (!ld_acquire_u32(&w.chunks[cb_k].plan_ready)) break;
-          cb_nb = ld_relaxed_u32(&w.chunks[cb_k].nb);
-          cb_ready = true;
-        }
-        const uint32_t j = atomicAdd(&w.chunks[cb_k].bticket, 1u);
-        if (j < cb_nb) {
-          d.kind = kItemB;
-          d.k = cb_k;
-          d.j = j;
-          return kItemB;
-        }
-        atomicCAS(&w.ctl->bchunk, cb_k, cb_k + 1u);
-        cb_k = max(cb_k + 1u, ld_acquire_u32(&w.ctl->bchunk));
-        cb_ready = false;
+  // thread 0: the next work, without waiting: B items of the current chunk
+  // (up to one per warp), else the next A tile whose Z slot is free
+  auto try_pick = [&]() -> uint32_t {
+    if (error_raised(ctrl)) return kDone;
+    for (;;) {
+      const uint32_t cb_k = s_cb_k;
+      if (cb_k >= w.K) break;
+      if (!s_cb_ready) {
+        if (!ld_acquire_u32(&w.chunks[cb_k].plan_ready)) break;
+        s_cb_nb = ld_relaxed_u32(&w.chunks[cb_k].nb);
+        s_cb_ready = 1u;
       }
-      if (held_a == kSent && ld_relaxed_u32(&w.ctl->aticket) < w.totalA) {
-        const uint32_t a = atomicAdd(&w.ctl->aticket, 1u);
-        if (a < w.totalA) held_a = a;
+      const uint32_t j0 = atomicAdd(&w.chunks[cb_k].bticket, (uint32_t)kWW);
+      const uint32_t nb = s_cb_nb;
+      if (j0 < nb) {
+        s_k = cb_k;
+        s_j0 = j0;
+        s_nj = min((uint32_t)kWW, nb - j0);
+        return kItemB;
       }
-      if (held_a != kSent) {
-        const uint32_t k = held_a / w.M;
-        bool free_slot = k < w.NZ;
-        if (!free_slot) {
-          const uint32_t kp = k - w.NZ;  // the chunk that used the slot before
-          free_slot = ld_acquire_u32(&w.chunks[kp].plan_ready) &&
-                      ld_acquire_u32(&w.chunks[kp].bdone) == ld_relaxed_u32(&w.chunks[kp].nb);
-        }
-        if (!free_slot) return kNone;
-        d.kind = kItemA;
-        d.k = k;
-        d.j = held_a % w.M;
-        d.len = min(kWE, n - held_a * kWE);
-        held_a = kSent;
-        return kItemA;
+      atomicCAS(&w.ctl->bchunk, cb_k, cb_k + 1u);
+      s_cb_k = max(cb_k + 1u, ld_acquire_u32(&w.ctl->bchunk));
+      s_cb_ready = 0u;
+    }
+    if (s_held_a == kSent && ld_relaxed_u32(&w.ctl->aticket) < w.totalA) {
+      const uint32_t a = atomicAdd(&w.ctl->aticket, 1u);
+      if (a < w.totalA) s_held_a = a;
+    }
+    const uint32_t held = s_held_a;
+    if (held != kSent) {
+      const uint32_t k = held / w.M;
+      bool free_slot = k < w.NZ;
+      if (!free_slot) {
+        const uint32_t kp = k - w.NZ;  // the chunk that used the slot before
+        free_slot = ld_acquire_u32(&w.chunks[kp].plan_ready) &&
+                    ld_acquire_u32(&w.chunks[kp].bdone) == ld_relaxed_u32(&w.chunks[kp].nb);
       }
-      return cb_k >= w.K ? kDone : kNone;
-    };
+      if (!free_slot) return kNone;
+      s_a = held;
+      s_held_a = kSent;
+      return kItemA;
+    }
+    return s_cb_k >= w.K ? kDone : kNone;
+  };
 
-    // B tile (k, j): bucket, its size and the running-prefix prefetch. Returns
-    // false while the bucket's earlier chunk has not folded its counts yet.
-    auto prepare_b = [&](ItemDesc& d) -> bool {
-      const uint32_t s = d.k % w.NZ;
-      if (plan_k != d.k) {
-        for (uint32_t x = lane; x < 257u; x += 32u) s_first[x] = ld_relaxed_u32(&w.first[s * kFirstStride + x]);
-        for (uint32_t x = lane; x < 256u; x += 32u) s_size[x] = ld_relaxed_u32(&w.S[(size_t)d.k * 256u + x]);
-        __syncwarp();
-        plan_k = d.k;
+  for (;;) {
+    if (tid == 0) {
+      uint32_t kind = try_pick();
+      if (kind == kNone && s_pending < 0) {
+        if (prof) s_prof[9] += 1ull;
+        const uint32_t idle = ++s_idle;
+        if (idle >= kSpinLimit || ((idle & 63u) == 0u && error_raised(ctrl))) {
+          record_error(ctrl, kStatusTimeout, kWhereSchedule);
+          kind = kDone;
+        } else {
+          __nanosleep(s_ns);
+          if (s_ns < 256) s_ns <<= 1;
+        }
+      } else if (kind != kNone) {
+        s_idle = 0;
+        s_ns = 8;
       }
-      uint32_t hit = 0, hh = 0;
+      s_kind = kind;
+    }
+    __syncthreads();
+    const uint32_t kind = s_kind;
+    if (kind == kDone) break;
+    if (kind == kNone) {  // nothing runnable: let this CTA's own A tile count first
+      flush();
+      continue;
+    }
+    mark(4);
+
+    if (kind == kItemA) {
+      // ---- A: sort one input tile by the high byte into its chunk's Z slot
+      bulk_wait_read_all();  // the previous A tile's copy has read the staging buffer
+      const uint32_t a = s_a, k = a / w.M, t = a % w.M, s = k % w.NZ;
+      const uint32_t begin = a * kWE, len = min(kWE, n - begin);
+      const bool full = len == kWE;
+      Elem v[kWK];
+      uint32_t r2[kWK / 2];
+      const Elem* p = src + begin + warp * 32u * kWK + lane;
 #pragma unroll
-      for (int r = 0; r < 8; r++) {
-        const uint32_t x = lane * 8u + r;
-        if (s_first[x] <= d.j && d.j < s_first[x + 1]) {
+      for (int q = 0; q < kWK; q++) {
+        const uint32_t pos = warp * 32u * kWK + (uint32_t)q * 32u + lane;
+        if (full || pos < len) v[q] = load_elem_stream(p + q * 32);
+        else v[q].key = v[q].val = 0;
+      }
+      if (full) rank_tile<true>(v, shift + 8, len, r2, wcnt, tcount, tstart, s_wt);
+      else rank_tile<false>(v, shift + 8, len, r2, wcnt, tcount, tstart, s_wt);
+#pragma unroll
+      for (int q = 0; q < kWK; q++)
+        if (full || warp * 32u * kWK + (uint32_t)q * 32u + lane < len)
+          buf[((r2[q / 2] >> ((q & 1) * 16)) & 0xFFFFu) +
+              wcnt[digit_of(v[q].key, shift + 8, 0xFFu) * kWWP + warp]] = v[q];
+      fence_proxy_async_smem();
+      __syncwarp();
+      for (uint32_t b = lane; b < 256u; b += 32u) wcnt[b * kWWP + warp] = 0u;
+      uint16_t* pt = w.PT + ((size_t)s * w.M + t) * kPTS;
+      if (tid < 256u) {
+        pt[tid] = (uint16_t)tstart[tid];
+        if (tcount[tid]) atomicAdd(&w.S[(size_t)k * 256u + tid], tcount[tid]);
+      } else if (tid == 256u) {
+        pt[256] = (uint16_t)len;
+      }
+      __syncthreads();
+      flush();  // the previous A tile (its copy has had this whole tile to drain)
+      if (tid == 0 && !error_raised(ctrl)) {
+        fence_proxy_async_global();
+        for (uint32_t off = 0; off < len; off += 2048u)
+          bulk_s2g(w.Z + (size_t)s * C + (size_t)t * kWE + off, smem_u32(buf + off),
+                   min(2048u, len - off) * (uint32_t)sizeof(Elem));
+        bulk_commit();
+      }
+      if (tid == 0) s_pending = (int32_t)k;
+      if (prof && tid == 0) s_prof[7] += 1ull;
+      mark(1);
+      continue;
+    }
+
+    // ---- B: one item per warp (bucket h of chunk k, or a part of it)
+    bulk_wait_read_all();  // an A tile's copy out of these bytes must be done reading them
+    __syncthreads();
+    const uint32_t k = s_k, s = k % w.NZ, mk = chunk_tiles(k);
+    if (s_plan_k != k) {
+      // the chunk's plan (first B item of each bucket) and bucket sizes
+      for (uint32_t x = tid; x < 257u; x += kWT) s_first[x] = ld_relaxed_u32(&w.first[s * kFirstStride + x]);
+      for (uint32_t x = tid; x < 256u; x += kWT) s_size[x] = ld_relaxed_u32(&w.S[(size_t)k * 256u + x]);
+      __syncthreads();
+      if (tid == 0) s_plan_k = k;
+    }
+    flush();
+    bool timed_out = false;
+    if (warp < s_nj) {
+      BWarp& me = bw[warp];
+      const uint32_t j = s_j0 + warp;
+      // the bucket of item j
+      uint32_t hh = 0, hit = 0;
+#pragma unroll
+      for (int rr = 0; rr < 8; rr++) {
+        const uint32_t x = lane * 8u + rr;
+        if (s_first[x] <= j && j < s_first[x + 1]) {
           hit = 1;
           hh = x;
         }
       }
-      const uint32_t src_lane = __ffs(__ballot_sync(0xffffffffu, hit)) - 1u;
-      d.h = __shfl_sync(0xffffffffu, hh, src_lane);
-      d.i = d.j - s_first[d.h];
-      d.J = s_first[d.h + 1] - s_first[d.h];
-      const uint32_t lo = d.i * kWE;
-      d.len = min(kWE, s_size[d.h] - lo);
-      // digit starts, and the running prefix for the bucket's first tile
-      bool ok = true;
-      if (d.i == 0) {
-        uint32_t kp = kSent;
-        if (lane == 0) {
-          int32_t q = (int32_t)d.k - 1;
-          while (q >= 0 && ld_relaxed_u32(&w.S[(size_t)q * 256u + d.h]) == 0u) q--;
-          kp = q < 0 ? kSent : (uint32_t)q;
-          ok = kp == kSent || ld_acquire_u32(&w.epoch[d.h]) >= kp + 1u;
+      const uint32_t h = __shfl_sync(0xffffffffu, hh, __ffs(__ballot_sync(0xffffffffu, hit)) - 1u);
+      const uint32_t i = j - s_first[h], J = s_first[h + 1] - s_first[h];
+      const uint32_t lo = i * kBQ, hi = min(s_size[h], lo + kBQ);
+      // the bucket's piece in every tile of the chunk, in tile order
+      uint32_t carry = 0;
+      for (uint32_t t0 = 0; t0 < mk; t0 += 32u) {
+        const uint32_t t = t0 + lane;
+        uint32_t c = 0, p0 = 0;
+        if (t < mk) {
+          const uint16_t* pt = w.PT + ((size_t)s * w.M + t) * kPTS;
+          p0 = ld_relaxed_u16(pt + h);
+          c = ld_relaxed_u16(pt + h + 1u) - p0;
         }
-        ok = __shfl_sync(0xffffffffu, (uint32_t)ok, 0) != 0;
-        if (!ok) return false;
-        __syncwarp();
-      }
-#pragma unroll
-      for (int r = 0; r < 8; r++) {
-        const uint32_t l = lane + 32u * r;
-        nx_pre[l] = d.i == 0 ? ld_relaxed_u32(&w.R[d.h * 256u + l]) : 0u;
-        nx_gst[l] = gstart[(d.h << 8) | l];
-      }
-      return true;
-    };
-
-    // bulk copies of item d into buffer b (after the buffer's last stores have read it)
-    auto issue_load = [&](const ItemDesc& d, uint32_t b) {
-      const uint32_t full = smem_u32(&s_full[b]);
-      Elem* tb = bufs + (size_t)b * kWE;
-      const uint32_t s = d.k % w.NZ;
-      if (lane == 0) mbar_arrive_expect_tx(full, d.len * (uint32_t)sizeof(Elem));
-      __syncwarp();
-      fence_proxy_async_global();
-      if (d.kind == kItemA) {
-        const uint32_t a = d.k * w.M + d.j;
-        const uint32_t q0 = lane * 2048u;
-        if (q0 < d.len)
-          bulk_g2s(smem_u32(tb + q0), src + (size_t)a * kWE + q0,
-                   min(2048u, d.len - q0) * (uint32_t)sizeof(Elem), full);
-      } else {
-        // the bucket's piece in every tile of the chunk: start, length, offset in the bucket
-        const uint32_t mk = chunk_tiles(d.k);
-        uint32_t p0[8], c[8], sum = 0;
-#pragma unroll
-        for (int r = 0; r < 8; r++) {
-          const uint32_t t = lane * 8u + r;
-          p0[r] = c[r] = 0;
-          if (t < mk) {
-            const uint16_t* pt = w.PT + ((size_t)s * w.M + t) * kPTS;
-            p0[r] = ld_relaxed_u16(pt + d.h);
-            c[r] = ld_relaxed_u16(pt + d.h + 1u) - p0[r];
-          }
-          sum += c[r];
-        }
-        uint32_t x = sum;
+        uint32_t x = c;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
           const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
           if (lane >= (uint32_t)o) x += y;
         }
-        uint32_t off = x - sum;
-        const uint32_t lo = d.i * kWE;
-#pragma unroll
-        for (int r = 0; r < 8; r++) {
-          const uint32_t t = lane * 8u + r;
-          const uint32_t a0 = max(off, lo), a1 = min(off + c[r], lo + d.len);
-          if (a0 < a1)
-            bulk_g2s(smem_u32(tb + (a0 - lo)), w.Z + (size_t)s * C + (size_t)t * kWE + p0[r] + (a0 - off),
-                     (a1 - a0) * (uint32_t)sizeof(Elem), full);
-          off += c[r];
+        if (t < mk) {
+          me.poff[t] = carry + x - c;
+          me.psrc[t] = t * kWE + p0;
         }
-#pragma unroll
-        for (int r = 0; r < 8; r++) {
-          pre[b * 256u + lane + 32u * r] = nx_pre[lane + 32u * r];
-          gst[b * 256u + lane + 32u * r] = nx_gst[lane + 32u * r];
-        }
+        carry += __shfl_sync(0xffffffffu, x, 31);
       }
-      if (lane == 0) s_desc[b] = d;
-      __syncwarp();
-      if (lane == 0) mbar_arrive(full);  // the description (and prefetches) are in place
-    };
-
-    // stores of the item staged in buffer b
-    auto issue_store = [&](uint32_t b) {
-      const ItemDesc d = s_desc[b];
-      Elem* tb = bufs + (size_t)b * kWE;
-      if (!error_raised(ctrl)) {
-        if (d.kind == kItemA) {
-          const uint32_t q0 = lane * 2048u;
-          if (q0 < d.len) {
-            fence_proxy_async_global();
-            bulk_s2g(w.Z + (size_t)(d.k % w.NZ) * C + (size_t)d.j * kWE + q0, smem_u32(tb + q0),
-                     min(2048u, d.len - q0) * (uint32_t)sizeof(Elem));
-          }
-        } else {
-#pragma unroll
-          for (int r = 0; r < 8; r++) {
-            const uint32_t l = lane + 32u * r;
-            const uint32_t cnt = tcount[b * 256u + l];
-            if (cnt) {
-              const uint32_t g = gbase[b * 256u + l];
-              if ((uint64_t)g + cnt > n) record_error(ctrl, kStatusInconsistent, kWhereScatter);
-              else bulk_s2g(dst + g, smem_u32(tb + tstart[b * 256u + l]), cnt * (uint32_t)sizeof(Elem));
-            }
-          }
-        }
-      }
-      bulk_commit();
-      // the group before this one is complete: its A tile can be signalled
-      bulk_wait_one();
-      __syncwarp();
-      if (pend_a_old >= 0) signal_a((uint32_t)pend_a_old);
-      pend_a_old = pend_a;
-      pend_a = d.kind == kItemA ? (int32_t)d.k : -1;
-    };
-
-    while (!failed) {
-      bool progress = false;
-      // 1. store every tile the compute warps have staged
-      while (it_store < it_load &&
-             mbar_test_wait(smem_u32(&s_staged[it_store & 1u]), (it_store >> 1) & 1u)) {
-        issue_store(it_store & 1u);
-        it_store++;
-        progress = true;
-      }
-      if (done && it_store == it_load) break;
-      // 2. choose the next item
-      if (!done && !have_nx) {
-        uint32_t kind = kNone;
-        if (lane == 0) {
-          kind = try_pick(nx);
-          if (kind == kDone) nx.kind = kDone;
-        }
-        kind = __shfl_sync(0xffffffffu, kind, 0);
-        if (kind != kNone) {
-          nx.kind = __shfl_sync(0xffffffffu, nx.kind, 0);
-          nx.k = __shfl_sync(0xffffffffu, nx.k, 0);
-          nx.j = __shfl_sync(0xffffffffu, nx.j, 0);
-          nx.len = __shfl_sync(0xffffffffu, nx.len, 0);
-          have_nx = true;
-          nx_pre_ok = nx.kind != kItemB;
-          progress = true;
-        }
-        pmark(4);
-      }
-      // 3. a B tile's bucket prefix (may have to wait for an earlier chunk)
-      if (have_nx && !nx_pre_ok) {
-        const long long e0 = clock64();
-        nx_pre_ok = prepare_b(nx);
-        if (prof && lane == 0) s_prof[5] += (unsigned long long)(clock64() - e0);
-        if (nx_pre_ok) progress = true;
-      }
-      // 4. load it once its buffer is free (the item two back has been stored and read out)
-      if (have_nx && nx_pre_ok && it_load < it_store + 2u) {
-        const uint32_t b = it_load & 1u;
-        if (it_load >= 2u) {
-          // the stores of item it_load - 2 (the newest or the second newest group) must have read the buffer
-          if (it_store - 1u == it_load - 2u) bulk_wait_read_all();
-          else bulk_wait_read_one();
-          __syncwarp();
-        }
-        if (nx.kind == kDone) {
-          // no more work: tell the compute warps (the marker is not an item)
-          if (lane == 0) {
-            s_desc[b].kind = kDone;
-            mbar_arrive(smem_u32(&s_full[b]));
-            mbar_arrive(smem_u32(&s_full[b]));
-          }
-          __syncwarp();
-          done = true;
-        } else {
-          issue_load(nx, b);
-          if (prof && lane == 0) s_prof[nx.kind == kItemA ? 7 : 8] += 1ull;
-          it_load++;
-        }
-        have_nx = false;
-        progress = true;
-      }
-      if (progress) {
-        idle = 0;
-        ns = 8;
-        continue;
-      }
-      // nothing to do: complete this CTA's pending A tiles first (their chunk
-      // plans may be what everybody waits for), then back off
-      if (pend_a >= 0 || pend_a_old >= 0) {
-        drain();
-        continue;
-      }
-      if (lane == 0 && prof) s_prof[9] += 1ull;
-      if (++idle >= kSpinLimit || ((idle & 63u) == 0u && error_raised(ctrl))) {
-        if (lane == 0 && !error_raised(ctrl)) record_error(ctrl, kStatusTimeout, kWhereSchedule);
-        failed = true;
-        break;
-      }
-      __nanosleep(ns);
-      if (ns < 256) ns <<= 1;
-    }
-    // (after a failure the compute warps' own bounded waits end them)
-    __syncwarp();
-    drain();
-    if (prof && lane == 0) {
-      s_prof[10] = (unsigned long long)(clock64() - t_start);
-      for (int f = 4; f < 12; f++) atomicAdd(&ctrl->wide_prof[pass][f], s_prof[f]);
-    }
-    return;
-  }
-
-  // =================== compute warps ===================
-  long long t_mark = clock64();
-  auto cmark = [&](int f) {
-    if (prof && tid == 0) {
-      const long long now = clock64();
-      s_prof[f] += (unsigned long long)(now - t_mark);
-      t_mark = now;
-    }
-  };
-  for (uint32_t it = 0;; it++) {
-    const uint32_t b = it & 1u;
-    const bool arrived = mbar_wait_bounded(smem_u32(&s_full[b]), (it >> 1) & 1u);
-    if (compute_sync_or(!arrived)) {
-      record_error(ctrl, kStatusTimeout, kWhereBulkCopy);
-      break;
-    }
-    cmark(0);
-    const ItemDesc d = s_desc[b];
-    if (d.kind == kDone) break;
-    Elem* tb = bufs + (size_t)b * kWE;
-    uint32_t* tc = tcount + b * 256u;
-    uint32_t* ts = tstart + b * 256u;
-    const bool full = d.len == kWE;
-    const int dshift = d.kind == kItemA ? shift + 8 : shift;
-    Elem v[kWK];
-    uint32_t r[kWK];
-#pragma unroll
-    for (int q = 0; q < kWK; q++) {
-      const uint32_t pos = warp * 32u * kWK + (uint32_t)q * 32u + lane;
-      if (full || pos < d.len) v[q] = lds_elem(tb + pos);
-      else v[q].key = v[q].val = 0;
-    }
-    if (full) rank_tile<true>(v, dshift, d.len, r, wcnt, tc, ts, s_wt);
-    else rank_tile<false>(v, dshift, d.len, r, wcnt, tc, ts, s_wt);
-    bool timed_out = false;
-    if (d.kind == kItemA) {
-      // piece table row and bucket sizes of the chunk
-      const uint32_t s = d.k % w.NZ;
-      uint16_t* pt = w.PT + ((size_t)s * w.M + d.j) * kPTS;
-      if (tid < 256u) {
-        pt[tid] = (uint16_t)ts[tid];
-        if (tc[tid]) atomicAdd(&w.S[(size_t)d.k * 256u + tid], tc[tid]);
-      } else if (tid == 256u) {
-        pt[256] = (uint16_t)d.len;
-      }
-    } else {
-      // elements of digit (h, tid) before this tile: the running prefix of
-      // earlier chunks (prefetched) plus earlier tiles of the bucket (look-back)
-      const uint32_t s = d.k % w.NZ;
-      const uint32_t tag = wide_tag(pass, d.k, d.j);
+      if (lane == 0) me.poff[mk] = carry;
+      // elements of digit (h, l) before this item: earlier chunks (R) and, for
+      // a bucket split over several items, the items before it (look-back)
+      const uint32_t tag = wide_tag(pass, k, j);
       uint64_t* ring = w.status + (size_t)s * w.nbmax * 256u;
-      uint64_t* my = ring + (size_t)d.j * 256u;
-      uint32_t excl = 0;
-      if (tid < 256u) {
-        if (d.i == 0) {
-          excl = pre[b * 256u + tid];
-          if (d.J > 1u) {
-            // the bucket's last tile overwrites R once its walk has seen this
-            // status: the read of R must be ordered before it
-            __threadfence();
-            st_relaxed_u64(my + tid, pack_status(kFlagIncl, tag, excl + tc[tid]));
+      uint64_t* my = ring + (size_t)j * 256u;
+      uint32_t excl[8];
+#pragma unroll
+      for (int rr = 0; rr < 8; rr++) excl[rr] = 0u;
+      if (i == 0) {
+        if (lane == 0) {
+          int32_t q = (int32_t)k - 1;
+          while (q >= 0 && ld_relaxed_u32(&w.S[(size_t)q * 256u + h]) == 0u) q--;
+          if (q >= 0) timed_out = wait_bucket_epoch(&w.epoch[h], (uint32_t)q + 1u, ctrl);
+        }
+        __syncwarp();
+#pragma unroll
+        for (int rr = 0; rr < 8; rr++) excl[rr] = ld_relaxed_u32(&w.R[h * 256u + lane + 32u * rr]);
+      }
+#pragma unroll
+      for (int rr = 0; rr < 8; rr++) me.cnt[lane + 32u * rr] = 0u;
+      __syncwarp();
+      // position pos of the bucket (lo <= pos < hi) lives at
+      // Z[psrc[t] + pos - poff[t]], t the piece holding it; each lane walks
+      // forward from the piece it used last
+      const Elem* Zs = w.Z + (size_t)s * C;
+      uint32_t pt_lane = first_piece(me.poff, mk, lo);
+      const uint32_t lt = lanemask_lt();
+      auto locate = [&](uint32_t pos) -> const Elem* {
+        while (me.poff[pt_lane + 1u] <= pos) pt_lane++;
+        return Zs + me.psrc[pt_lane] + (pos - me.poff[pt_lane]);
+      };
+      const bool split = J > 1u;
+      if (split) {
+        // a bucket split over several items: count this item's elements by
+        // low byte, publish the counts, resolve the items before it
+        for (uint32_t b0 = lo; b0 < hi; b0 += 32u) {
+          const uint32_t pos = b0 + lane;
+          const bool valid = pos < hi;
+          uint32_t l = 0;
+          if (valid) l = digit_of(load_elem_cg(locate(pos)).key, shift, 0xFFu);
+          const uint32_t peers = warp_peers(l, 8, valid);
+          if (valid && (peers & lt) == 0u) me.cnt[l] += __popc(peers);  // the first peer adds for all
+          __syncwarp();
+        }
+        pt_lane = first_piece(me.poff, mk, lo);
+        if (i == 0) {
+          // the bucket's first item: prefix = R; published inclusive (the
+          // bucket's last item overwrites R once its walk has seen this)
+          __threadfence();
+#pragma unroll
+          for (int rr = 0; rr < 8; rr++) {
+            const uint32_t l = lane + 32u * rr;
+            st_relaxed_u64(my + l, pack_status(kFlagIncl, tag, excl[rr] + me.cnt[l]));
           }
         } else {
-          st_relaxed_u64(my + tid, pack_status(kFlagAgg, tag, tc[tid]));
-          timed_out = walk_bucket(ring, d.j, tid, pass, d.k, ctrl, &excl);
-          st_relaxed_u64(my + tid, pack_status(kFlagIncl, tag, excl + tc[tid]));
+#pragma unroll
+          for (int rr = 0; rr < 8; rr++) {
+            const uint32_t l = lane + 32u * rr;
+            st_relaxed_u64(my + l, pack_status(kFlagAgg, tag, me.cnt[l]));
+          }
+#pragma unroll
+          for (int rr = 0; rr < 8; rr++) {
+            const uint32_t l = lane + 32u * rr;
+            uint32_t e = 0;
+            if (walk_bucket(ring, j, l, pass, k, ctrl, &e)) timed_out = true;
+            excl[rr] = e;
+            st_relaxed_u64(my + l, pack_status(kFlagIncl, tag, e + me.cnt[l]));
+          }
         }
-        gbase[b * 256u + tid] = gst[b * 256u + tid] + excl;
       }
-      if (d.i + 1u == d.J) {
-        // the bucket's last tile: hand the running prefix on to the next chunk
-        __threadfence();
-        if (tid < 256u) st_relaxed_u32(&w.R[d.h * 256u + tid], excl + tc[tid]);
-        compute_sync();
-        if (tid == 0) {
-          __threadfence();
-          st_release_u32(&w.epoch[d.h], d.k + 1u);
+#pragma unroll
+      for (int rr = 0; rr < 8; rr++) {
+        const uint32_t l = lane + 32u * rr;
+        me.gbase[l] = gstart[(h << 8) | l] + excl[rr];
+        me.cnt[l] = 0u;
+      }
+      __syncwarp();
+      if (!__any_sync(0xffffffffu, timed_out)) {
+        // place the elements: kBU rounds of 32 loaded ahead, ranked in order
+        for (uint32_t b0 = lo; b0 < hi; b0 += 32u * kBU) {
+          Elem e[kBU];
+#pragma unroll
+          for (int u = 0; u < kBU; u++) {
+            const uint32_t pos = b0 + (uint32_t)u * 32u + lane;
+            if (pos < hi) e[u] = load_elem_cg(locate(pos));
+            else e[u].key = e[u].val = 0;
+          }
+#pragma unroll
+          for (int u = 0; u < kBU; u++) {
+            const uint32_t pos = b0 + (uint32_t)u * 32u + lane;
+            const bool valid = pos < hi;
+            if (!__any_sync(0xffffffffu, valid)) break;
+            const uint32_t l = valid ? digit_of(e[u].key, shift, 0xFFu) : 0u;
+            const uint32_t peers = warp_peers(l, 8, valid);
+            uint32_t c = 0;
+            if (valid) c = me.cnt[l];
+            __syncwarp();
+            if (valid) {
+              me.cnt[l] = c + __popc(peers);  // every peer writes the same count
+              const uint32_t o = me.gbase[l] + c + __popc(peers & lt);
+              if (o < n) store_elem(dst + o, e[u]);
+              else record_error(ctrl, kStatusInconsistent, kWhereScatter);
+            }
+            __syncwarp();
+          }
+        }
+        if (i + 1u == J) {
+          // the bucket's last item: hand the running prefix on to the next chunk
+          // (after a look-back, its reads must be ordered before the overwrite)
+          if (split) __threadfence();
+#pragma unroll
+          for (int rr = 0; rr < 8; rr++) {
+            const uint32_t l = lane + 32u * rr;
+            st_relaxed_u32(&w.R[h * 256u + l], excl[rr] + me.cnt[l]);
+          }
+          __syncwarp();
+          if (lane == 0) {
+            __threadfence();
+            st_release_u32(&w.epoch[h], k + 1u);
+          }
         }
       }
-      if (compute_sync_or(timed_out)) break;
-      if (tid == 0) {
+      if (lane == 0) {
         __threadfence();
-        atomicAdd(&w.chunks[d.k].bdone, 1u);  // done with Z, the piece table and the ring slot
+        atomicAdd(&w.chunks[k].bdone, 1u);  // done with Z, the piece table and the ring slot
       }
     }
-    compute_sync();  // every item of the tile is in registers: the buffer is free for staging
-#pragma unroll
-    for (int q = 0; q < kWK; q++)
-      if (full || warp * 32u * kWK + (uint32_t)q * 32u + lane < d.len)
-        tb[r[q] + wcnt[digit_of(v[q].key, dshift, 0xFFu) * kWWP + warp]] = v[q];
-    fence_proxy_async_smem();
-    __syncwarp();
-    for (uint32_t bin = lane; bin < 256u; bin += 32u) wcnt[bin * kWWP + warp] = 0u;
-    compute_sync();
-    if (tid == 0) mbar_arrive(smem_u32(&s_staged[b]));
-    cmark(d.kind == kItemA ? 1 : 2);
+    if (__syncthreads_or(timed_out)) break;
+    if (prof && tid == 0) s_prof[8] += s_nj;
+    mark(2);
   }
+  flush();
+  bulk_wait_all();
   if (prof && tid == 0) {
-    for (int f = 0; f < 4; f++) atomicAdd(&ctrl->wide_prof[pass][f], s_prof[f]);
+    s_prof[10] = (unsigned long long)(clock64() - s_t_start);
+    for (int f = 0; f < 12; f++) atomicAdd(&ctrl->wide_prof[pass][f], s_prof[f]);
   }
 }
 
@@ -1140,7 +1006,7 @@ void wide_geometry(uint32_t n, uint32_t* M, uint32_t* NZ, uint32_t* K, uint32_t*
   *M = std::max(min_m, env_u32("LSB_WIDE_CHUNK_TILES", 128, 4, 256));
   *NZ = env_u32("LSB_WIDE_SLOTS", 3, 2, 8);
   *K = (*totalA + *M - 1) / *M;
-  *nbmax = *M + 256u;
+  *nbmax = 256u + (*M * kWE + kBQ - 1u) / kBQ;
 }
 
 uint32_t wide_tile_elems() { return kWE; }
@@ -1168,7 +1034,8 @@ size_t wide_layout_bytes(uint32_t n, size_t* pass_zero_bytes, size_t* ring_bytes
 }
 
 static size_t wide_smem() {
-  return 2u * (size_t)kWE * sizeof(Elem) + 256u * kWWP * 4u + 5u * 512u * 4u + 2u * 256u * 4u;
+  static_assert(sizeof(BWarp) * kWW <= (size_t)kWE * sizeof(Elem), "B state fits the staging buffer");
+  return (size_t)kWE * sizeof(Elem) + 256u * kWWP * 4u + 2u * 256u * 4u;
 }
 
 int wide_run(Elem* X, Elem* Y, int first_digit, int target_parity, unsigned char* ws,

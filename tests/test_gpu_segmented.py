@@ -87,6 +87,17 @@ def test_autotuner_returns_a_candidate(lsb, cuda):
     off = np.zeros(len(sizes) + 1, dtype=np.int64)
     off[1:] = np.cumsum(sizes)
     t = lsb.tune_segmented(off)
-    assert (t.digit_bits, t.variant) in {(8, 0), (8, 2), (11, 0), (11, 2)}
+    sms = cuda.cuda.get_device_properties(0).multi_processor_count
+    # digit width 8, 11 or 16; kernel shape 0 or 2; all resident CTAs, one per SM or half the SMs
+    assert t.digit_bits in (8, 11, 16) and t.variant in (0, 2) and t.ctas in (0, sms, max(1, sms // 2))
     t2 = lsb.tune_segmented(off)  # cached per size class
-    assert (t2.digit_bits, t2.variant) == (t.digit_bits, t.variant)
+    assert (t2.digit_bits, t2.variant, t2.ctas) == (t.digit_bits, t.variant, t.ctas)
+    # the chosen configuration sorts the batch like the default one
+    a = lsb.generate(int(off[-1]), lsb.DIST_UNIFORM, 3)
+    A, B = a.clone(), cuda.empty_like(a)
+    offs = cuda.from_numpy(off).cuda()
+    ws = lsb.alloc_segmented_workspace(int(off[-1]), len(sizes), t.digit_bits)
+    lsb.sort_segmented(A, B, offs, t, ws)
+    A2 = a.clone()
+    lsb.sort_segmented(A2, B, offs, None, lsb.alloc_segmented_workspace(int(off[-1]), len(sizes), 8))
+    assert cuda.equal(A, A2)

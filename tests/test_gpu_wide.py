@@ -12,7 +12,7 @@ from conftest import to_dev, to_np
 
 pytestmark = pytest.mark.gpu
 
-TILE = 6144  # elements per tile of the wide kernel
+TILE = 8192  # elements per A tile of the wide kernel
 
 
 @pytest.fixture(autouse=True)
