@@ -85,6 +85,11 @@ def args_parse(argv=None):
     p.add_argument("--requests", type=int, default=10000)
     p.add_argument("--rate", type=float, default=400.0, help="Poisson arrival rate, requests/s")
     p.add_argument("--serve-slots", type=int, default=4)
+    p.add_argument("--no-serve-sweep", dest="serve_sweep", action="store_false",
+                   help="skip the arrival-rate sweep of the serving leg")
+    p.add_argument("--sweep-requests", type=int, default=1500)
+    p.add_argument("--host-requests", type=int, default=1000)
+    p.add_argument("--host-rate", type=float, default=1000.0)
     return p.parse_args(argv)
 
 
@@ -551,42 +556,100 @@ def segmented_leg(args, lsb, torch, ranks) -> dict:
     }
 
 
-def serving_leg(args, lsb, torch, ranks) -> dict:
-    """Open-loop request stream: Poisson arrivals at args.rate, sizes
-    floor(2^U(10, 27)) elements of uniform keys (generated on the device per
-    request), 16-bit digits, through the request loop (lsb_server_*)."""
-    import numpy as np
-
-    rng = np.random.default_rng(7 + ranks.rank)
-    sizes = np.floor(2.0 ** rng.uniform(10, 27, size=args.requests)).astype(np.int64)
-    arrivals = np.cumsum(rng.exponential(1.0 / args.rate, size=args.requests))
-    with lsb.Server(slots=args.serve_slots, digit_bits=16) as srv:
+def _serve_run(lsb, srv_kwargs: dict, n_req: int, arrivals, submit) -> dict:
+    """One open-loop run: submits request i at arrivals[i] (seconds after the
+    start) through `submit(srv, i)`, waits for every result, and returns the
+    host-side and device-side statistics."""
+    with lsb.Server(**srv_kwargs) as srv:
         t0 = time.perf_counter()
         ids = []
-        for i in range(args.requests):
+        for i in range(n_req):
             delay = t0 + arrivals[i] - time.perf_counter()
             if delay > 0.002:
                 time.sleep(delay - 0.001)
             while time.perf_counter() < t0 + arrivals[i]:
                 pass
-            ids.append(srv.submit_generated(int(sizes[i]), 0, 1 + i))
-        batched = 0
+            ids.append(submit(srv, i))
         for r in ids:
             info = srv.wait(r)
             if info.status != 0:
                 raise RuntimeError(f"request {r} failed with status {info.status}")
-            batched += info.batch > 1
-        st = srv.stats()
-    return {
-        "requests": args.requests, "rate_per_s": args.rate, "size_law": "floor(2^U(10,27))",
-        "elements": int(sizes.sum()), "slots": args.serve_slots, "digit_bits": 16,
-        "latency_p50_ms": round(st.latency_p50_ms, 3), "latency_p99_ms": round(st.latency_p99_ms, 3),
-        "service_p50_ms": round(st.service_p50_ms, 3), "service_p99_ms": round(st.service_p99_ms, 3),
-        "value": round(st.elements_per_s / 1e6, 3), "unit": UNIT, "wall_ms": round(st.wall_ms, 1),
-        "batched_requests": int(st.batched_requests), "units": int(st.units),
-        "peak_hbm_gb": round(st.peak_bytes / 1e9, 3), "budget_hbm_gb": round(st.budget_bytes / 1e9, 3),
-        "offered_melem_s": round(float(sizes.mean()) * args.rate / 1e6, 1),
-    }
+        return {"stats": srv.stats(), "device": srv.device_stats()}
+
+
+def _serve_summary(res: dict, n_req: int, rate: float, elements: int, size_law: str) -> dict:
+    st, dv = res["stats"], res["device"]
+    return {"requests": n_req, "rate_per_s": rate, "size_law": size_law, "elements": int(elements),
+            "latency_p50_ms": round(st.latency_p50_ms, 3), "latency_p99_ms": round(st.latency_p99_ms, 3),
+            "service_p50_ms": round(st.service_p50_ms, 3), "service_p99_ms": round(st.service_p99_ms, 3),
+            "value": round(st.elements_per_s / 1e6, 3), "unit": UNIT, "wall_ms": round(st.wall_ms, 1),
+            "batched_requests": int(st.batched_requests), "units": int(st.units),
+            "peak_hbm_gb": round(st.peak_bytes / 1e9, 3), "budget_hbm_gb": round(st.budget_bytes / 1e9, 3),
+            "device_overlap": round(dv.overlap, 3), "device_max_concurrent_units": int(dv.max_concurrent),
+            "device_busy_ms": round(dv.busy_ms, 1)}
+
+
+def serving_leg(args, lsb, torch, ranks) -> dict:
+    """Open-loop request streams through the request loop (lsb_server_*),
+    16-bit digits:
+      - the configuration: Poisson arrivals at args.rate, args.requests
+        requests, sizes floor(2^U(10, 27)) elements of uniform keys generated
+        on the device per request;
+      - a sweep of the arrival rate with the same size law up to saturation
+        (served against offered load and p99 per rate);
+      - host-buffer requests (pinned host memory copied in and out by the
+        loop), sizes floor(2^U(10, 20)).
+    The units' device spans (CUDA events on their streams) show whether units
+    on different stream slots overlap on the GPU (device_overlap > 1)."""
+    import numpy as np
+
+    kw = {"slots": args.serve_slots, "digit_bits": 16}
+    rng = np.random.default_rng(7 + ranks.rank)
+    sizes = np.floor(2.0 ** rng.uniform(10, 27, size=args.requests)).astype(np.int64)
+    arrivals = np.cumsum(rng.exponential(1.0 / args.rate, size=args.requests))
+    res = _serve_run(lsb, kw, args.requests, arrivals,
+                     lambda srv, i: srv.submit_generated(int(sizes[i]), 0, 1 + i))
+    out = _serve_summary(res, args.requests, args.rate, sizes.sum(), "floor(2^U(10,27))")
+    out["offered_melem_s"] = round(float(sizes.mean()) * args.rate / 1e6, 1)
+    out["slots"] = args.serve_slots
+    out["digit_bits"] = 16
+
+    if args.serve_sweep:
+        sweep = []
+        for rate in (200.0, 400.0, 800.0, 1600.0, 3200.0, 6400.0):
+            m = args.sweep_requests
+            rs = np.random.default_rng(100 + int(rate))
+            sz = np.floor(2.0 ** rs.uniform(10, 27, size=m)).astype(np.int64)
+            arr = np.cumsum(rs.exponential(1.0 / rate, size=m))
+            r = _serve_run(lsb, kw, m, arr, lambda srv, i, sz=sz: srv.submit_generated(int(sz[i]), 0, 1 + i))
+            row = _serve_summary(r, m, rate, sz.sum(), "floor(2^U(10,27))")
+            row["offered_melem_s"] = round(float(sz.mean()) * rate / 1e6, 1)
+            sweep.append(row)
+        out["sweep"] = sweep
+        out["saturation_melem_s"] = max(x["value"] for x in sweep)
+        base_p99 = sweep[0]["latency_p99_ms"]
+        out["p99_knee_rate_per_s"] = next(
+            (x["rate_per_s"] for x in sweep
+             if x["latency_p99_ms"] > 10 * base_p99 or x["value"] < 0.9 * x["offered_melem_s"]), None)
+
+    # requests whose data lives in host memory (pinned), copied in and out by the loop
+    m = args.host_requests
+    rh = np.random.default_rng(9)
+    hs = np.floor(2.0 ** rh.uniform(10, 20, size=m)).astype(np.int64)
+    off = np.zeros(m + 1, dtype=np.int64)
+    off[1:] = np.cumsum(hs)
+    host = torch.empty((int(off[-1]), 2), dtype=torch.int64, pin_memory=True)
+    # non-negative keys, so that the signed check below agrees with the unsigned order
+    host[:, 0] = torch.randint(0, 1 << 62, (int(off[-1]),), dtype=torch.int64)
+    host[:, 1] = torch.arange(int(off[-1]), dtype=torch.int64)
+    arr = np.cumsum(rh.exponential(1.0 / args.host_rate, size=m))
+    views = [host[off[i]:off[i + 1]] for i in range(m)]
+    r = _serve_run(lsb, kw, m, arr, lambda srv, i: srv.submit_host(views[i]))
+    hrow = _serve_summary(r, m, args.host_rate, hs.sum(), "floor(2^U(10,20)), pinned host buffers")
+    hrow["sorted_check"] = all(bool((v[1:, 0] >= v[:-1, 0]).all()) for v in views[:: max(1, m // 50)])
+    out["host_buffers"] = hrow
+    del host, views
+    return out
 
 
 def main(argv=None):

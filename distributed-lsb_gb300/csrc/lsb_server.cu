@@ -60,6 +60,7 @@ struct Unit {
   bool b_ws_freed = false;
   Clock::time_point t_done;
   std::atomic<int> gpu_done{0};  // set by the stream callback
+  cudaEvent_t ev_start = nullptr, ev_end = nullptr;  // the unit's span on its stream
 };
 
 struct Server {
@@ -83,6 +84,9 @@ struct Server {
   int64_t elements_done = 0, requests_done = 0, units_done = 0, batched_requests = 0;
   Clock::time_point t_first{}, t_last{};
   bool have_first = false;
+  // device spans of finished units, ms after ref_event (the server's creation)
+  cudaEvent_t ref_event = nullptr;
+  std::vector<std::pair<float, float>> spans;
 };
 
 size_t unit_bytes(const lsb_server_config_t& cfg, int64_t n_total, int64_t nseg, size_t* ws_out) {
@@ -126,6 +130,9 @@ int launch_unit(Server* s, Unit* u) {
   if (rc == LSB_OK) rc = alloc_from_pool(s, &u->ws, ws_bytes, st);
   if (rc == LSB_OK && k > 1) rc = alloc_from_pool(s, (void**)&u->d_off, (size_t)(k + 1) * 8u, st);
   if (rc != LSB_OK) return rc;
+  if (cudaEventCreate(&u->ev_start) != cudaSuccess || cudaEventCreate(&u->ev_end) != cudaSuccess ||
+      cudaEventRecord(u->ev_start, st) != cudaSuccess)
+    return LSB_ERR_CUDA;
   // inputs
   for (Request* r : u->reqs) {
     lsb_elem_t* dst = u->d_a + r->unit_offset;
@@ -158,6 +165,7 @@ int launch_unit(Server* s, Unit* u) {
         cudaMemcpyAsync(r->host, u->d_a + r->unit_offset, (size_t)r->n * sizeof(lsb_elem_t),
                         cudaMemcpyDeviceToHost, st) != cudaSuccess)
       return LSB_ERR_CUDA;
+  if (cudaEventRecord(u->ev_end, st) != cudaSuccess) return LSB_ERR_CUDA;
   if (cudaLaunchHostFunc(st, on_unit_done, u) != cudaSuccess) return LSB_ERR_CUDA;
   return LSB_OK;
 }
@@ -191,7 +199,16 @@ void worker_loop(Server* s) {
       if (u->d_b) cudaFreeAsync(u->d_b, st);
       if (u->ws) cudaFreeAsync(u->ws, st);
       if (u->d_off) cudaFreeAsync(u->d_off, st);
+      float t0 = 0.f, t1 = 0.f;
+      const bool timed = u->ev_start && u->ev_end && u->gpu_done.load(std::memory_order_acquire) &&
+                         cudaEventElapsedTime(&t0, s->ref_event, u->ev_start) == cudaSuccess &&
+                         cudaEventElapsedTime(&t1, s->ref_event, u->ev_end) == cudaSuccess;
+      if (u->ev_start) cudaEventDestroy(u->ev_start);
+      if (u->ev_end) cudaEventDestroy(u->ev_end);
+      u->ev_start = u->ev_end = nullptr;
+      cudaGetLastError();
       lk.lock();
+      if (timed) s->spans.emplace_back(t0, t1);
       u->b_ws_freed = true;
       s->running[u->slot] = nullptr;
       for (Request* r : u->reqs) {
@@ -327,6 +344,12 @@ int lsb_server_create(const lsb_server_config_t* cfg, lsb_server_t** out) {
     s->running.push_back(nullptr);
   }
   if (s->cfg.batch_max_requests <= 0) s->cfg.batch_max_requests = (int32_t)maxb;
+  if (cudaEventCreate(&s->ref_event) != cudaSuccess ||
+      cudaEventRecord(s->ref_event, s->streams[0]) != cudaSuccess ||
+      cudaEventSynchronize(s->ref_event) != cudaSuccess) {
+    delete s;
+    return LSB_ERR_CUDA;
+  }
   s->worker = std::thread(worker_loop, s);
   *out = s;
   return LSB_OK;
@@ -430,6 +453,45 @@ int lsb_server_fetch(lsb_server_t* s, uint64_t id, lsb_elem_t* h_out, int64_t n)
     s->cv_work.notify_all();
   }
   return rc;
+}
+
+int lsb_server_device_stats(lsb_server_t* s, lsb_server_device_stats_t* out) {
+  if (!s || !out) return LSB_ERR_INVALID_ARG;
+  std::vector<std::pair<float, float>> sp;
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    sp = s->spans;
+  }
+  std::memset(out, 0, sizeof *out);
+  out->units_timed = (int64_t)sp.size();
+  if (sp.empty()) return LSB_OK;
+  // union of the spans, and the most spans open at one instant (an end
+  // sorts before a start at the same time)
+  std::vector<std::pair<double, int>> ev;
+  double sum = 0.0;
+  for (auto& x : sp) {
+    sum += (double)x.second - x.first;
+    ev.emplace_back(x.first, +1);
+    ev.emplace_back(x.second, -1);
+  }
+  std::sort(ev.begin(), ev.end());
+  int open = 0, peak = 0;
+  double busy = 0.0, since = 0.0;
+  for (auto& e : ev) {
+    if (e.second > 0) {
+      if (open == 0) since = e.first;
+      open++;
+      peak = std::max(peak, open);
+    } else {
+      open--;
+      if (open == 0) busy += e.first - since;
+    }
+  }
+  out->busy_ms = busy;
+  out->unit_ms_sum = sum;
+  out->overlap = busy > 0.0 ? sum / busy : 0.0;
+  out->max_concurrent = peak;
+  return LSB_OK;
 }
 
 int lsb_server_stats(lsb_server_t* s, lsb_server_stats_t* out) {

@@ -64,6 +64,7 @@ SIGNATURES = {
     "lsb_server_wait": (ctypes.c_int, [_P, ctypes.c_uint64, ctypes.c_double, _P]),
     "lsb_server_fetch": (ctypes.c_int, [_P, ctypes.c_uint64, _P, _I64]),
     "lsb_server_stats": (ctypes.c_int, [_P, _P]),
+    "lsb_server_device_stats": (ctypes.c_int, [_P, _P]),
     "lsb_server_destroy": (ctypes.c_int, [_P]),
     "lsb_profile_enable": (ctypes.c_int, [ctypes.c_int]),
     "lsb_profile_read": (ctypes.c_int, [_P, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]),
@@ -311,6 +312,13 @@ class SegmentedGraph:
             pass
 
 
+class ServerDeviceStats(ctypes.Structure):
+    """lsb_server_device_stats_t"""
+
+    _fields_ = [("units_timed", ctypes.c_int64), ("busy_ms", ctypes.c_double), ("unit_ms_sum", ctypes.c_double),
+                ("overlap", ctypes.c_double), ("max_concurrent", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+
+
 class Server:
     """The request loop (lsb_server_*): continuous batching of sort requests."""
 
@@ -351,6 +359,11 @@ class Server:
     def stats(self) -> ServerStats:
         st = ServerStats()
         _check(load().lsb_server_stats(self.handle, ctypes.byref(st)), "lsb_server_stats")
+        return st
+
+    def device_stats(self) -> ServerDeviceStats:
+        st = ServerDeviceStats()
+        _check(load().lsb_server_device_stats(self.handle, ctypes.byref(st)), "lsb_server_device_stats")
         return st
 
     def close(self) -> None:

@@ -250,6 +250,17 @@ int lsb_server_wait(lsb_server_t* server, uint64_t id, double timeout_s, lsb_req
 /* Copies a kept result to host memory and releases it. */
 int lsb_server_fetch(lsb_server_t* server, uint64_t id, lsb_elem_t* h_out, int64_t n);
 int lsb_server_stats(lsb_server_t* server, lsb_server_stats_t* out);
+/* Device-side view of the same run: every unit's span on its stream (from its
+ * first copy or generation to its last copy back), timed with CUDA events. */
+typedef struct lsb_server_device_stats {
+  int64_t units_timed;
+  double busy_ms;         /* time during which at least one unit was on the device */
+  double unit_ms_sum;     /* sum of the units' spans                               */
+  double overlap;         /* unit_ms_sum / busy_ms: 1 = one unit at a time         */
+  int32_t max_concurrent; /* most units on the device at one instant               */
+  int32_t reserved;
+} lsb_server_device_stats_t;
+int lsb_server_device_stats(lsb_server_t* server, lsb_server_device_stats_t* out);
 /* Finishes every submitted request, then frees everything. */
 int lsb_server_destroy(lsb_server_t* server);
 
