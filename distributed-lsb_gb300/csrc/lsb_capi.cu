@@ -423,6 +423,24 @@ int lsb_sort_pairs(lsb_elem_t* d_a, lsb_elem_t* d_b, int64_t n, int digit_bits, 
                       lsb_num_passes(digit_bits), 0, d_workspace, workspace_bytes, st);
 }
 
+// A 12-, 14- or 16-bit pass as two half-width sub-passes through scratch:
+// the layout of the sub-passes, and the bytes of layout plus scratch.
+static bool pass_split_layout(int64_t n, int digit_bits, Layout* L, size_t* bytes) {
+  if (!(digit_bits == 12 || digit_bits == 14 || digit_bits == 16) || wide_mode() != WideMode::kSplit)
+    return false;
+  if (plan_layout(n, digit_bits, 1, L, true) != 0 || L->sub != 2 || L->num_digits != 2) return false;
+  *bytes = align_up(L->total, 256) + (size_t)n * sizeof(Elem);
+  return true;
+}
+
+int lsb_pass_workspace_bytes(int64_t n, int digit_bits, size_t* bytes) {
+  if (int rc = lsb_workspace_bytes(n, digit_bits, bytes)) return rc;
+  Layout L;
+  size_t split = 0;
+  if (pass_split_layout(n, digit_bits, &L, &split)) *bytes = std::max(*bytes, split);
+  return LSB_OK;
+}
+
 int lsb_pass(const lsb_elem_t* d_src, lsb_elem_t* d_dst, int64_t n, int digit_bits, int digit,
              void* d_workspace, size_t workspace_bytes, void* stream) {
   if (int rc = check_common(d_src, d_dst, n, digit_bits)) return rc;
@@ -432,6 +450,36 @@ int lsb_pass(const lsb_elem_t* d_src, lsb_elem_t* d_dst, int64_t n, int digit_bi
     if (d_workspace && cudaMemsetAsync(d_workspace, 0, kCtrlBytes, st) != cudaSuccess)
       return LSB_ERR_CUDA;
     return LSB_OK;
+  }
+  // wide digits: two half-width sub-passes src -> scratch -> dst, when the
+  // caller's workspace holds the scratch (lsb_pass_workspace_bytes) or the
+  // library allocates it
+  Layout Ls;
+  size_t split_bytes = 0;
+  if (pass_split_layout(n, digit_bits, &Ls, &split_bytes) &&
+      (d_workspace ? workspace_bytes >= split_bytes : workspace_bytes == 0)) {
+    if (d_workspace && ((uintptr_t)d_workspace & 255u)) return LSB_ERR_WORKSPACE;
+    void* w = d_workspace;
+    if (!w)
+      if (int rc = pool_alloc(&w, split_bytes, st)) return rc;
+    unsigned char* wb = static_cast<unsigned char*>(w);
+    Elem* mid = reinterpret_cast<Elem*>(wb + align_up(Ls.total, 256));
+    int rc = LSB_OK;
+    if (cudaMemsetAsync(wb, 0, kCtrlBytes, st) != cudaSuccess) rc = LSB_ERR_CUDA;
+    if (rc == LSB_OK) {
+      const int r = onesweep_pass_via(reinterpret_cast<const Elem*>(d_src), mid,
+                                      reinterpret_cast<Elem*>(d_dst), digit * 2, wb, Ls, st);
+      if (r) rc = r == 1 ? LSB_ERR_INVALID_ARG : LSB_ERR_CUDA;
+    }
+    if (d_workspace) return rc;
+    uint32_t dev_err = 0;
+    if (rc == LSB_OK &&
+        cudaMemcpyAsync(&dev_err, w, sizeof(uint32_t), cudaMemcpyDeviceToHost, st) != cudaSuccess)
+      rc = LSB_ERR_CUDA;
+    cudaFreeAsync(w, st);
+    if (cudaStreamSynchronize(st) != cudaSuccess && rc == LSB_OK) rc = LSB_ERR_CUDA;
+    if (rc == LSB_OK && dev_err) rc = (int)dev_err;
+    return rc;
   }
   // X = src is only ever read: one pass reads X and writes Y, or, when the
   // digit is constant, the final copy moves X into Y.

@@ -81,6 +81,10 @@ int task_run(Elem* X, Elem* Y, int first_digit, int target_parity, unsigned char
              const Layout& L, cudaStream_t st);
 int wide_run(Elem* X, Elem* Y, int first_digit, int target_parity, unsigned char* ws,
              const Layout& L, cudaStream_t st);
+// One wide digit as two half-width onesweep passes src -> mid -> dst (L: a
+// split layout of two sub-digits starting at first_digit); src is not written.
+int onesweep_pass_via(const Elem* src, Elem* mid, Elem* dst, int first_digit, unsigned char* ws,
+                      const Layout& L, cudaStream_t st);
 // Bytes of the wide family's pass region for n elements; offs[0..8] receive
 // the offsets of its parts, *pass_zero_bytes the size of the leading part
 // that is cleared before every pass and *ring_bytes that of the status ring.

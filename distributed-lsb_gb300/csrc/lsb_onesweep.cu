@@ -1115,4 +1115,56 @@ int onesweep_run(Elem* X, Elem* Y, int first_digit, int target_parity, unsigned 
   return final_copy(X, Y, L.n, L.num_digits, target_parity, ctrl, st);
 }
 
+// One wide digit (12, 14 or 16 bits) from src into dst as two stable
+// half-width passes through `mid` (src -> mid -> dst), src untouched. Both
+// sub-passes run even when a sub-digit is constant (then that pass is a plain
+// stable copy), so that the result lands in dst whatever the digits.
+__global__ void k_two_passes(Ctrl* ctrl) {
+  if (threadIdx.x != 0) return;
+  ctrl->skip_mask_lo = 0u;
+  ctrl->skip_mask_hi = 0u;
+  ctrl->parity[0] = 0u;
+  ctrl->parity[1] = 1u;
+  ctrl->parity[2] = 0u;
+  ctrl->passes_run = 2u;
+  ctrl->final_copy = 0u;
+}
+
+int onesweep_pass_via(const Elem* src, Elem* mid, Elem* dst, int first_digit, unsigned char* ws,
+                      const Layout& L, cudaStream_t st) {
+  Ctrl* ctrl = reinterpret_cast<Ctrl*>(ws);
+  uint32_t* hist = reinterpret_cast<uint32_t*>(ws + L.off_hist);
+  uint32_t* gstart = reinterpret_cast<uint32_t*>(ws + L.off_gstart);
+  uint64_t* ring = reinterpret_cast<uint64_t*>(ws + L.off_ring);
+  uint32_t* done = reinterpret_cast<uint32_t*>(ws + L.off_done);
+  const uint32_t nbins = 1u << L.bits;
+  const uint32_t tiles = (L.n + L.tile_elems - 1) / L.tile_elems;
+  const uint32_t used_slots = std::min(tiles, L.ring_tiles);
+  if (L.num_digits != 2) return 1;
+  if (cudaMemsetAsync(ring, 0, (size_t)used_slots * nbins * 8u, st) != cudaSuccess) return 5;
+  if (cudaMemsetAsync(done, 0, (size_t)L.ring_tiles * 4u, st) != cudaSuccess) return 5;
+  if (int rc = histogram_u32(src, L.n, L.bits, first_digit, 2, hist, st)) return rc;
+  {
+    ProfScope prof("plan", st);
+    k_plan<<<1, kPlanThreads, 0, st>>>(hist, gstart, L.n, L.bits, 2, 0, L.api_bits, L.sub, ctrl);
+    k_two_passes<<<1, 32, 0, st>>>(ctrl);
+  }
+  if (cudaPeekAtLastError() != cudaSuccess) return 5;
+  const OnesweepChoice c = onesweep_choice(L.bits);
+  Elem* in = const_cast<Elem*>(src);  // read only: pass 0 has parity 0 and reads X
+  {
+    ProfScope prof("onesweep_scatter", st);
+    c.kern<<<L.grid, c.threads, c.smem, st>>>(in, mid, L.n, L.bits, 0, first_digit, gstart, ring, done,
+                                              L.ring_tiles, ctrl, SegDesc{});
+  }
+  if (cudaPeekAtLastError() != cudaSuccess) return 5;
+  {
+    // parity 1: reads Y = mid, writes X = dst
+    ProfScope prof("onesweep_scatter", st);
+    c.kern<<<L.grid, c.threads, c.smem, st>>>(dst, mid, L.n, L.bits, 1, first_digit + 1, gstart + nbins,
+                                              ring, done, L.ring_tiles, ctrl, SegDesc{});
+  }
+  return cudaPeekAtLastError() == cudaSuccess ? 0 : 5;
+}
+
 }  // namespace lsb

@@ -222,22 +222,39 @@ __global__ void __launch_bounds__(kH16Threads)
 #pragma unroll
     for (int u = 0; u < kH16Unroll; u++)
       key[u] = load_elem_stream(data + base + (uint64_t)u * 32u + lane).key;
+    // All the round's counter additions are issued before any of their
+    // returned words is looked at, so that their shared-memory round trips
+    // overlap; the rare carries are repaired afterwards.
+    constexpr int kHalf = kH16Unroll / 2;
 #pragma unroll
-    for (int u = 0; u < kH16Unroll; u++) {
-      // bits in which some lane's key differs from lane 0's: a digit whose
-      // bits are all clear there is the same in the whole warp (skewed
-      // inputs), and lane 0 counts all 32 at once
-      const uint64_t x = key[u] ^ __shfl_sync(0xffffffffu, key[u], 0);
-      const uint64_t diff = ((uint64_t)__reduce_or_sync(0xffffffffu, (uint32_t)(x >> 32)) << 32) |
-                            __reduce_or_sync(0xffffffffu, (uint32_t)x);
+    for (int h0 = 0; h0 < kH16Unroll; h0 += kHalf) {
+      uint32_t old[kHalf][ND], inc[kHalf][ND], dig[kHalf][ND];
 #pragma unroll
-      for (int dd = 0; dd < ND; dd++) {
-        const int shift = 16 * (first_digit + dd);
-        const uint32_t d = digit_of(key[u], shift, 0xFFFFu);
-        if (digit_of(diff, shift, 0xFFFFu) == 0u) {
-          if (lane == 0) byte_count(cw + dd * 16384, d, 32u, ghist + (size_t)dd * 65536u);
-        } else {
-          byte_count(cw + dd * 16384, d, 1u, ghist + (size_t)dd * 65536u);
+      for (int uu = 0; uu < kHalf; uu++) {
+        const int u = h0 + uu;
+        // bits in which some lane's key differs from lane 0's: a digit whose
+        // bits are all clear there is the same in the whole warp (skewed
+        // inputs), and lane 0 counts all 32 at once
+        const uint64_t x = key[u] ^ __shfl_sync(0xffffffffu, key[u], 0);
+        const uint64_t diff = ((uint64_t)__reduce_or_sync(0xffffffffu, (uint32_t)(x >> 32)) << 32) |
+                              __reduce_or_sync(0xffffffffu, (uint32_t)x);
+#pragma unroll
+        for (int dd = 0; dd < ND; dd++) {
+          const int shift = 16 * (first_digit + dd);
+          const uint32_t d = digit_of(key[u], shift, 0xFFFFu);
+          const uint32_t v = digit_of(diff, shift, 0xFFFFu) == 0u ? (lane == 0 ? 32u : 0u) : 1u;
+          dig[uu][dd] = d;
+          inc[uu][dd] = v;
+          old[uu][dd] = v ? atomicAdd(&cw[dd * 16384 + (d >> 2)], v << ((d & 3u) * 8u)) : 0u;
+        }
+      }
+#pragma unroll
+      for (int uu = 0; uu < kHalf; uu++) {
+#pragma unroll
+        for (int dd = 0; dd < ND; dd++) {
+          const uint32_t d = dig[uu][dd], v = inc[uu][dd];
+          if (((old[uu][dd] >> ((d & 3u) * 8u)) & 0xFFu) + v >= 256u)
+            byte_carry_fix(old[uu][dd], d, ghist + (size_t)dd * 65536u);
         }
       }
     }
@@ -263,7 +280,7 @@ __global__ void __launch_bounds__(kH16Threads)
 
 constexpr int kHCThreads = 512;
 constexpr uint32_t kHCStage = 1024;  // elements per stage (16 KiB)
-constexpr int kHCStages = 4;
+constexpr int kHCStages = 6;
 
 __device__ __forceinline__ uint32_t cluster_ctarank() {
   uint32_t r;
@@ -344,32 +361,39 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kHCThreads, 1)
     __syncthreads();
     if (s_bad) break;
     const Elem* st = stage + (size_t)b * kHCStage;
+    // all of the stage's counter additions of this thread first, then the
+    // (rare) carry repairs, so that the shared-memory round trips overlap
+    constexpr int kQ = (int)(kHCStage / kHCThreads);
+    uint32_t old[kQ][2], inc[kQ][2], dig[kQ][2];
 #pragma unroll
-    for (uint32_t q = 0; q < kHCStage / kHCThreads; q++) {
-      const uint32_t pos = q * kHCThreads + threadIdx.x;  // a warp reads 32 consecutive elements
+    for (int q = 0; q < kQ; q++) {
+      const uint32_t pos = (uint32_t)q * kHCThreads + threadIdx.x;  // a warp reads 32 consecutive elements
       const bool valid = pos < len;
       const uint64_t key = valid ? st[pos].key : 0ull;
-      if (__all_sync(0xffffffffu, valid)) {
-        const uint64_t x = key ^ __shfl_sync(0xffffffffu, key, 0);
-        const uint64_t diff = ((uint64_t)__reduce_or_sync(0xffffffffu, (uint32_t)(x >> 32)) << 32) |
-                              __reduce_or_sync(0xffffffffu, (uint32_t)x);
+      // bits in which some lane's key differs from lane 0's (whole warp valid):
+      // a digit whose bits are all clear there is counted 32 at once by lane 0
+      const bool all = __all_sync(0xffffffffu, valid);
+      const uint64_t x = key ^ __shfl_sync(0xffffffffu, key, 0);
+      const uint64_t diff = ((uint64_t)__reduce_or_sync(0xffffffffu, (uint32_t)(x >> 32)) << 32) |
+                            __reduce_or_sync(0xffffffffu, (uint32_t)x);
 #pragma unroll
-        for (int dd = 0; dd < 2; dd++) {
-          const int shift = 16 * (first_digit + 2 * (int)rank + dd);
-          const uint32_t d = digit_of(key, shift, 0xFFFFu);
-          if (digit_of(diff, shift, 0xFFFFu) == 0u) {
-            if (lane == 0) byte_count(cw + dd * 16384, d, 32u, g0 + (size_t)dd * 65536u);
-          } else {
-            byte_count(cw + dd * 16384, d, 1u, g0 + (size_t)dd * 65536u);
-          }
-        }
-      } else if (valid) {
-#pragma unroll
-        for (int dd = 0; dd < 2; dd++)
-          byte_count(cw + dd * 16384, digit_of(key, 16 * (first_digit + 2 * (int)rank + dd), 0xFFFFu), 1u,
-                     g0 + (size_t)dd * 65536u);
+      for (int dd = 0; dd < 2; dd++) {
+        const int shift = 16 * (first_digit + 2 * (int)rank + dd);
+        const uint32_t d = digit_of(key, shift, 0xFFFFu);
+        const uint32_t v = !valid ? 0u
+                           : (all && digit_of(diff, shift, 0xFFFFu) == 0u) ? (lane == 0 ? 32u : 0u)
+                                                                           : 1u;
+        dig[q][dd] = d;
+        inc[q][dd] = v;
+        old[q][dd] = v ? atomicAdd(&cw[dd * 16384 + (d >> 2)], v << ((d & 3u) * 8u)) : 0u;
       }
     }
+#pragma unroll
+    for (int q = 0; q < kQ; q++)
+#pragma unroll
+      for (int dd = 0; dd < 2; dd++)
+        if (((old[q][dd] >> ((dig[q][dd] & 3u) * 8u)) & 0xFFu) + inc[q][dd] >= 256u)
+          byte_carry_fix(old[q][dd], dig[q][dd], g0 + (size_t)dd * 65536u);
     __syncthreads();
     if (threadIdx.x == 0) {
       // both consumers (this CTA and its peer) are done with buffer b

@@ -44,6 +44,7 @@ SIGNATURES = {
     "lsb_workspace_bytes": (ctypes.c_int, [_I64, ctypes.c_int, ctypes.POINTER(ctypes.c_size_t)]),
     "lsb_sort_pairs": (ctypes.c_int, [_P, _P, _I64, ctypes.c_int, _P, ctypes.c_size_t, _P]),
     "lsb_pass": (ctypes.c_int, [_P, _P, _I64, ctypes.c_int, ctypes.c_int, _P, ctypes.c_size_t, _P]),
+    "lsb_pass_workspace_bytes": (ctypes.c_int, [_I64, ctypes.c_int, ctypes.POINTER(ctypes.c_size_t)]),
     "lsb_histogram": (ctypes.c_int, [_P, _I64, ctypes.c_int, _P, _P]),
     "lsb_query": (ctypes.c_int, [_P, _P, _P]),
     "lsb_sort_pairs_host": (ctypes.c_int, [_P, _I64, ctypes.c_int, _P]),
@@ -201,6 +202,13 @@ def sort_pairs(a, b, digit_bits: int = 16, workspace=None, stream=None) -> None:
     wsb = workspace.numel() if workspace is not None else 0
     _check(load().lsb_sort_pairs(_ptr(a), _ptr(b), n, digit_bits, ws, wsb, _stream_ptr(stream)),
            "lsb_sort_pairs")
+
+
+def pass_workspace_bytes(n: int, digit_bits: int) -> int:
+    """Workspace of lsb_pass at its fastest (scratch for wide-digit sub-passes)."""
+    out = ctypes.c_size_t(0)
+    _check(load().lsb_pass_workspace_bytes(n, digit_bits, ctypes.byref(out)), "lsb_pass_workspace_bytes")
+    return out.value
 
 
 def global_shuffle(src, dst, digit: int, digit_bits: int = 16, workspace=None, stream=None) -> None:

@@ -107,8 +107,20 @@ int lsb_workspace_bytes(int64_t n, int digit_bits, size_t* bytes);
 int lsb_sort_pairs(lsb_elem_t* d_a, lsb_elem_t* d_b, int64_t n, int digit_bits,
                    void* d_workspace, size_t workspace_bytes, void* stream);
 
+/* Workspace for lsb_pass at its fastest: for 12-, 14- and 16-bit digits it
+ * adds room for n elements of scratch (16 B each), through which the pass runs
+ * as two stable half-width sub-passes (src -> scratch -> dst); for other
+ * widths it equals lsb_workspace_bytes. */
+int lsb_pass_workspace_bytes(int64_t n, int digit_bits, size_t* bytes);
+
 /* One pass: d_dst = d_src stably sorted by digit `digit` (bits
  * [digit*b, digit*b + b) of the key). d_src is not modified.
+ * A 12-, 14- or 16-bit digit runs as two half-width sub-passes through n
+ * elements of scratch when the workspace holds them (at least
+ * lsb_pass_workspace_bytes) or is NULL (the library allocates the scratch);
+ * with a workspace of only lsb_workspace_bytes it runs as one pass of the
+ * task kernel family (the reference's count / scan / shuffle structure),
+ * several times slower.
  * Replaces globalShuffle(A, B, digit) (mpi/mpi_lsbsort.cpp:493-589): the
  * reference shuffles A into B locally and then places the result back in A;
  * here source and destination are explicit, so a caller that wants the

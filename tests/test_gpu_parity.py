@@ -69,6 +69,33 @@ def test_pass_matches_reference_golden(lsb, cuda, oracle, golden):
             assert digest(to_np(cur)) == c["after_pass_sha256"][d], (c["dist"], c["n"], d)
 
 
+@pytest.mark.parametrize("bits", [16, 14, 12])
+def test_wide_digit_pass_workspaces(lsb, cuda, oracle, bits):
+    """A wide-digit pass gives the same bytes through each of its routes: two
+    half-width sub-passes through scratch the library allocates (no
+    workspace) or the caller's workspace holds (lsb_pass_workspace_bytes),
+    and one task-family pass (a workspace of lsb_workspace_bytes only); the
+    source stays untouched. Constant sub-digits included (low32, equal)."""
+    import torch
+
+    for dist, n in ((oracle.DIST_UNIFORM, 300007), (oracle.DIST_ZIPF, 100003), (oracle.DIST_LOW32, 65537),
+                    (oracle.DIST_EQUAL, 4097), (oracle.DIST_NEARLY_SORTED, 1 << 18)):
+        a = oracle.generate(n, dist, 13)
+        src = to_dev(a, cuda)
+        big = torch.empty(lsb.pass_workspace_bytes(n, bits), dtype=torch.uint8, device="cuda")
+        small = lsb.alloc_workspace(n, bits)
+        for d in range(oracle.num_passes(bits)):
+            exp = oracle.global_shuffle(a, d, bits)
+            for ws in (None, big, small):
+                dst = cuda.empty_like(src)
+                lsb.global_shuffle(src, dst, d, bits, workspace=ws)
+                cuda.cuda.synchronize()
+                if ws is not None:
+                    assert lsb.query(ws).device_status == 0
+                assert np.array_equal(to_np(dst), exp), (bits, dist, d, None if ws is None else ws.numel())
+            assert np.array_equal(to_np(src), a)
+
+
 @pytest.mark.parametrize("bits", [8, 11])
 def test_pass_matches_oracle(lsb, cuda, oracle, bits):
     for dist in DISTS:
