@@ -26,6 +26,13 @@ Prints ONE JSON line (rank 0):
                graph-captured sort against a loop of lsb_sort_pairs
   serving      10^4 Poisson-arrival requests through the request loop:
                latency p50/p99 and elements/s
+  digit_bits_8 / digit_bits_11 / single_pass_task_family /
+  single_pass_wide_family
+               the same sort through the other digit widths and kernel
+               families (all give the same bytes)
+  histogram_b16
+               lsb_histogram at 16-bit digits: one HBM read by CTA pairs
+               against one read per three digits
 
 --impl reference times the reference algorithm on the host cores instead
 (see cpu_arm below). --gpus N (torchrun) runs N independent replicas, one
@@ -451,6 +458,9 @@ def gpu_arm(args, ranks: Ranks):
             out["digit_bits_11"] = time_sorts(11)
         if bits in (12, 14, 16):
             out["single_pass_task_family"] = time_sorts(bits, reps=2, env={"LSB_WIDE_DIGITS": "task"})
+        if bits == 16:
+            out["single_pass_wide_family"] = time_sorts(bits, reps=2, env={"LSB_WIDE_DIGITS": "wide"})
+            out["histogram_b16"] = histogram_b16_leg(lsb, torch, A)
 
     if not args.no_configs:
         out["configs"] = configs_leg(args, lsb, torch, peaks)
@@ -513,6 +523,38 @@ def gpu_arm(args, ranks: Ranks):
                                "one_rank": {"value": round(val1, 3), "unit": UNIT, "cores": 1,
                                             "sample": f"{one} uniform elements, 16-bit digits, one rank"}}
     return out
+
+
+def histogram_b16_leg(lsb, torch, data, reps: int = 3) -> dict:
+    """lsb_histogram at 16-bit digits (four digits of every key) in its two
+    forms: CTA pairs over one HBM read of the keys (default), and one read per
+    three digits. Kernel time from the library's own launch events; the counts
+    of both forms must agree."""
+    res, counts = {}, {}
+    for form in ("pairs", "split"):
+        old = os.environ.get("LSB_HIST16")
+        os.environ["LSB_HIST16"] = form
+        try:
+            lsb.histogram(data, 16)  # warm-up
+            torch.cuda.synchronize()
+            lsb.profile_read()
+            lsb.profile_enable(True)
+            for _ in range(reps):
+                h = lsb.histogram(data, 16)
+            torch.cuda.synchronize()
+            lsb.profile_enable(False)
+            prof = lsb.profile_read()
+        finally:
+            if old is None:
+                os.environ.pop("LSB_HIST16", None)
+            else:
+                os.environ["LSB_HIST16"] = old
+        launches, total = prof.get("hist16", (0, 0.0))
+        counts[form] = h
+        res[form] = {"ms": round(total / reps, 4), "launches": launches // reps,
+                     "hbm_reads_of_keys": 1 if form == "pairs" else 2}
+    res["counts_agree"] = bool(torch.equal(counts["pairs"], counts["split"]))
+    return res
 
 
 def segmented_leg(args, lsb, torch, ranks) -> dict:

@@ -516,19 +516,11 @@ int lsb_histogram(const lsb_elem_t* d_data, int64_t n, int digit_bits, int64_t* 
     return rc;
   }
   if (digit_bits == 16) {
-    // byte-packed counters: one read of the keys per three digits
+    // byte-packed counters: all four digits in one HBM read of the keys
     void* tmp = nullptr;
     const uint32_t cnt = (uint32_t)P * nbins;
-    if (int rc = pool_alloc(&tmp, (size_t)cnt * 4u + kCtrlBytes, st)) return rc;
-    if (cudaMemsetAsync(static_cast<unsigned char*>(tmp) + (size_t)cnt * 4u, 0, kCtrlBytes, st) != cudaSuccess) {
-      cudaFreeAsync(tmp, st);
-      return LSB_ERR_CUDA;
-    }
-    // the control block of the one-read form sits behind the counts
-    int rc = hist16(data, (uint32_t)n, 0, P, (uint32_t*)tmp, st,
-                    reinterpret_cast<Ctrl*>(static_cast<unsigned char*>(tmp) + (size_t)cnt * 4u))
-                 ? LSB_ERR_CUDA
-                 : LSB_OK;
+    if (int rc = pool_alloc(&tmp, (size_t)cnt * 4u, st)) return rc;
+    int rc = hist16(data, (uint32_t)n, 0, P, (uint32_t*)tmp, st) ? LSB_ERR_CUDA : LSB_OK;
     if (rc == LSB_OK) {
       k_u32_to_i64<<<(cnt + 255) / 256, 256, 0, st>>>((uint32_t*)tmp, d_counts, cnt);
       if (cudaPeekAtLastError() != cudaSuccess) rc = LSB_ERR_CUDA;

@@ -205,19 +205,41 @@ __device__ __forceinline__ void byte_flush(const uint32_t* words, uint32_t* g) {
 constexpr int kH16Threads = 512;
 constexpr int kH16Unroll = 8;
 
+// paired == 0: the CTAs share the whole array (grid-stride) and count digits
+// [first_digit, first_digit + ND). paired == 1: CTAs 2p and 2p+1 walk the
+// same contiguous range of the array side by side, CTA 2p counting digits
+// [first_digit, +ND) and CTA 2p+1 the ND digits after them, so that the
+// second read of every key is served by L2: 2*ND digits in one HBM read
+// without the shared memory for all of them in one CTA.
 template <int ND>
 __global__ void __launch_bounds__(kH16Threads)
     k_hist16(const Elem* __restrict__ data, uint32_t n, int first_digit,
-             uint32_t* __restrict__ ghist) {
+             uint32_t* __restrict__ ghist, uint32_t paired) {
   extern __shared__ uint32_t cw[];  // [ND][16384]
   for (uint32_t i = threadIdx.x; i < ND * 16384u; i += blockDim.x) cw[i] = 0u;
   __syncthreads();
   const uint32_t lane = lane_id();
-  const uint64_t warps_total = (uint64_t)gridDim.x * (blockDim.x >> 5);
-  const uint64_t gw = (uint64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   const uint64_t chunk = 32u * kH16Unroll;
-  const uint64_t full_end = (uint64_t)n / chunk * chunk;
-  for (uint64_t base = gw * chunk; base < full_end; base += warps_total * chunk) {
+  uint64_t lo = 0, hi = n, warps_total, gw, threads_total, gt;
+  if (paired) {
+    const uint32_t role = blockIdx.x & 1u, pairs = gridDim.x >> 1, pair = blockIdx.x >> 1;
+    first_digit += (int)role * ND;
+    ghist += (size_t)role * ND * 65536u;
+    const uint64_t per = ((uint64_t)n + pairs - 1) / pairs;
+    lo = std::min<uint64_t>((uint64_t)pair * per, n);
+    hi = std::min<uint64_t>(lo + per, n);
+    warps_total = blockDim.x >> 5;
+    gw = threadIdx.x >> 5;
+    threads_total = blockDim.x;
+    gt = threadIdx.x;
+  } else {
+    warps_total = (uint64_t)gridDim.x * (blockDim.x >> 5);
+    gw = (uint64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    threads_total = (uint64_t)gridDim.x * blockDim.x;
+    gt = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  }
+  const uint64_t full_end = lo + (hi - lo) / chunk * chunk;
+  for (uint64_t base = lo + gw * chunk; base < full_end; base += warps_total * chunk) {
     uint64_t key[kH16Unroll];
 #pragma unroll
     for (int u = 0; u < kH16Unroll; u++)
@@ -259,8 +281,7 @@ __global__ void __launch_bounds__(kH16Threads)
       }
     }
   }
-  for (uint64_t i = full_end + (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-       i += (uint64_t)gridDim.x * blockDim.x) {
+  for (uint64_t i = full_end + gt; i < hi; i += threads_total) {
     const uint64_t k = load_elem_stream(data + i).key;
 #pragma unroll
     for (int dd = 0; dd < ND; dd++)
@@ -272,175 +293,34 @@ __global__ void __launch_bounds__(kH16Threads)
   for (int dd = 0; dd < ND; dd++) byte_flush(cw + dd * 16384, ghist + (size_t)dd * 65536u);
 }
 
-// ---------------------------------------------------------------------------
-// histogram of four 16-bit digits in one read: a cluster of two CTAs, each
-// holding the byte counters of two digits (128 KiB), fed by multicast bulk
-// copies so that every key is read from memory once and lands in both CTAs'
-// shared memory
-
-constexpr int kHCThreads = 512;
-constexpr uint32_t kHCStage = 1024;  // elements per stage (16 KiB)
-constexpr int kHCStages = 6;
-
-__device__ __forceinline__ uint32_t cluster_ctarank() {
-  uint32_t r;
-  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
-  return r;
-}
-// the same shared-memory offset in CTA `rank` of the cluster
-__device__ __forceinline__ uint32_t map_shared(uint32_t addr, uint32_t rank) {
-  uint32_t r;
-  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(addr), "r"(rank));
-  return r;
-}
-__device__ __forceinline__ void mbar_arrive_cluster(uint32_t cluster_addr) {
-  asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];" ::"r"(cluster_addr)
-               : "memory");
-}
-// bulk copy of `bytes` from global memory into the same offset of every CTA
-// in `mask`, completing on each one's barrier at offset `bar`
-__device__ __forceinline__ void bulk_g2s_multicast(uint32_t dst, const void* src, uint32_t bytes,
-                                                   uint32_t bar, uint16_t mask) {
-  asm volatile(
-      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes.multicast::cluster"
-      " [%0], [%1], %2, [%3], %4;" ::"r"(dst),
-      "l"(src), "r"(bytes), "r"(bar), "h"(mask)
-      : "memory");
-}
-__device__ __forceinline__ void cluster_sync_all() {
-  asm volatile("barrier.cluster.arrive.release.aligned;\nbarrier.cluster.wait.acquire.aligned;" ::: "memory");
-}
-
-__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kHCThreads, 1)
-    k_hist16_cluster(const Elem* __restrict__ data, uint32_t n, int first_digit,
-                     uint32_t* __restrict__ ghist, Ctrl* ctrl) {
-  extern __shared__ __align__(16) unsigned char smem[];
-  uint32_t* cw = reinterpret_cast<uint32_t*>(smem);                           // [2][16384]
-  Elem* stage = reinterpret_cast<Elem*>(smem + 2u * 16384u * 4u);             // [kHCStages][kHCStage]
-  __shared__ __align__(8) uint64_t s_full[kHCStages], s_empty[kHCStages];
-  __shared__ uint32_t s_bad;
-  const uint32_t rank = cluster_ctarank(), peer = rank ^ 1u;
-  const uint32_t lane = lane_id();
-  for (uint32_t i = threadIdx.x; i < 2u * 16384u; i += blockDim.x) cw[i] = 0u;
-  if (threadIdx.x == 0) {
-    s_bad = 0u;
-    for (int b = 0; b < kHCStages; b++) {
-      mbar_init(smem_u32(&s_full[b]), 1);   // this CTA's expect_tx arrival (+ both halves' bytes)
-      mbar_init(smem_u32(&s_empty[b]), 2);  // both CTAs' consumers
-    }
-    fence_mbar_init();
-  }
-  __syncthreads();
-  cluster_sync_all();  // both CTAs' barriers exist before any copy or remote arrival
-  // this cluster's contiguous range of elements
-  const uint32_t clusters = gridDim.x / 2u, c = blockIdx.x / 2u;
-  const uint64_t per = ((uint64_t)n + clusters - 1) / clusters;
-  const uint64_t lo64 = (uint64_t)c * per, hi64 = lo64 + per;
-  const uint32_t lo = (uint32_t)(lo64 < n ? lo64 : n);
-  const uint32_t hi = (uint32_t)(hi64 < n ? hi64 : n);
-  const uint32_t nst = (hi - lo + kHCStage - 1) / kHCStage;
-  auto stage_len = [&](uint32_t i) { return min(kHCStage, hi - lo - i * kHCStage); };
-  // thread 0: this CTA's half of stage i into buffer i % kHCStages of both CTAs
-  auto issue = [&](uint32_t i) {
-    const uint32_t b = i % kHCStages, len = stage_len(i);
-    const uint32_t half = min(len, kHCStage / 2u);
-    const uint32_t e0 = rank == 0 ? 0u : half, e1 = rank == 0 ? half : len;
-    const uint32_t full = smem_u32(&s_full[b]);
-    mbar_arrive_expect_tx(full, len * (uint32_t)sizeof(Elem));
-    if (e1 > e0)
-      bulk_g2s_multicast(smem_u32(stage + (size_t)b * kHCStage + e0), data + lo + (size_t)i * kHCStage + e0,
-                         (e1 - e0) * (uint32_t)sizeof(Elem), full, (uint16_t)0x3);
-  };
-  if (threadIdx.x == 0)
-    for (uint32_t i = 0; i < nst && i < (uint32_t)kHCStages; i++) issue(i);
-  uint32_t* g0 = ghist + (size_t)(2u * rank) * 65536u;
-  for (uint32_t i = 0; i < nst; i++) {
-    const uint32_t b = i % kHCStages, len = stage_len(i);
-    const bool ok = mbar_wait_bounded(smem_u32(&s_full[b]), (i / kHCStages) & 1u);
-    if (!ok) atomicOr(&s_bad, 1u);
-    __syncthreads();
-    if (s_bad) break;
-    const Elem* st = stage + (size_t)b * kHCStage;
-    // all of the stage's counter additions of this thread first, then the
-    // (rare) carry repairs, so that the shared-memory round trips overlap
-    constexpr int kQ = (int)(kHCStage / kHCThreads);
-    uint32_t old[kQ][2], inc[kQ][2], dig[kQ][2];
-#pragma unroll
-    for (int q = 0; q < kQ; q++) {
-      const uint32_t pos = (uint32_t)q * kHCThreads + threadIdx.x;  // a warp reads 32 consecutive elements
-      const bool valid = pos < len;
-      const uint64_t key = valid ? st[pos].key : 0ull;
-      // bits in which some lane's key differs from lane 0's (whole warp valid):
-      // a digit whose bits are all clear there is counted 32 at once by lane 0
-      const bool all = __all_sync(0xffffffffu, valid);
-      const uint64_t x = key ^ __shfl_sync(0xffffffffu, key, 0);
-      const uint64_t diff = ((uint64_t)__reduce_or_sync(0xffffffffu, (uint32_t)(x >> 32)) << 32) |
-                            __reduce_or_sync(0xffffffffu, (uint32_t)x);
-#pragma unroll
-      for (int dd = 0; dd < 2; dd++) {
-        const int shift = 16 * (first_digit + 2 * (int)rank + dd);
-        const uint32_t d = digit_of(key, shift, 0xFFFFu);
-        const uint32_t v = !valid ? 0u
-                           : (all && digit_of(diff, shift, 0xFFFFu) == 0u) ? (lane == 0 ? 32u : 0u)
-                                                                           : 1u;
-        dig[q][dd] = d;
-        inc[q][dd] = v;
-        old[q][dd] = v ? atomicAdd(&cw[dd * 16384 + (d >> 2)], v << ((d & 3u) * 8u)) : 0u;
-      }
-    }
-#pragma unroll
-    for (int q = 0; q < kQ; q++)
-#pragma unroll
-      for (int dd = 0; dd < 2; dd++)
-        if (((old[q][dd] >> ((dig[q][dd] & 3u) * 8u)) & 0xFFu) + inc[q][dd] >= 256u)
-          byte_carry_fix(old[q][dd], dig[q][dd], g0 + (size_t)dd * 65536u);
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      // both consumers (this CTA and its peer) are done with buffer b
-      const uint32_t e = smem_u32(&s_empty[b]);
-      mbar_arrive_cluster(map_shared(e, rank));
-      mbar_arrive_cluster(map_shared(e, peer));
-      if (i + kHCStages < nst) {
-        // refill it once the peer is done with it too
-        if (!mbar_wait_bounded(e, (i / kHCStages) & 1u)) atomicOr(&s_bad, 1u);
-        else issue(i + kHCStages);
-      }
-    }
-  }
-  if (s_bad) record_error(ctrl, kStatusTimeout, kWhereBulkCopy);
-  __syncthreads();
-  // no CTA leaves while its peer may still copy into it or arrive on its barriers
-  cluster_sync_all();
-  byte_flush(cw, g0);
-  byte_flush(cw + 16384, g0 + 65536u);
-}
-
 // Counts of 16-bit digits [first_digit, first_digit + num_digits) into
-// d_counts[num_digits][65536] (uint32; zeroed here). Four digits: one read of
-// the keys by clusters of two CTAs; otherwise one read per three digits.
-static bool hist16_cluster_enabled() {
-  const char* e = std::getenv("LSB_HIST16_CLUSTER");
-  return !(e && e[0] == '0');
+// d_counts[num_digits][65536] (uint32; zeroed here). Four digits: one HBM read
+// of the keys by CTA pairs (two digits per CTA, the pair's second read of a
+// key served by L2); otherwise, or with LSB_HIST16=split, one read per three
+// digits. Both forms give the same counts in about the same time (7.7 and
+// 7.5 ms for four digits of 2^30 keys on a GB300: the counting instructions,
+// not the reads, bound both).
+static bool hist16_split() {
+  const char* e = std::getenv("LSB_HIST16");
+  return e && std::strcmp(e, "split") == 0;
 }
 
 int hist16(const Elem* data, uint32_t n, int first_digit, int num_digits, uint32_t* d_counts,
-           cudaStream_t st, Ctrl* ctrl) {
+           cudaStream_t st) {
   DeviceInfo dev;
   if (int rc = current_device_info(&dev)) return rc;
   if (cudaMemsetAsync(d_counts, 0, (size_t)num_digits * 65536u * 4u, st) != cudaSuccess) return 5;
   if (n == 0) return 0;
-  if (num_digits == 4 && ctrl && hist16_cluster_enabled() && dev.sm_count >= 2) {
-    const size_t smem = 2u * 65536u + (size_t)kHCStages * kHCStage * sizeof(Elem);
-    if (cudaFuncSetAttribute(k_hist16_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) ==
-        cudaSuccess) {
-      // one cluster of two CTAs per pair of SMs, no more than the work needs
-      const uint64_t want = ((uint64_t)n + 4u * kHCStage - 1) / (4u * kHCStage);
-      const uint32_t clusters = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(want, (uint64_t)dev.sm_count / 2u));
-      ProfScope prof("hist16", st);
-      k_hist16_cluster<<<2u * clusters, kHCThreads, smem, st>>>(data, n, first_digit, d_counts, ctrl);
-      if (cudaPeekAtLastError() == cudaSuccess) return 0;
-    }
-    cudaGetLastError();  // no cluster launch here: count with the per-CTA kernels
+  if (num_digits == 4 && !hist16_split() && dev.sm_count >= 2) {
+    const size_t smem = 2u * 65536u;
+    if (cudaFuncSetAttribute(k_hist16<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+        cudaSuccess)
+      return 5;
+    const uint64_t want = ((uint64_t)n + 8u * kH16Threads * kH16Unroll - 1) / (8u * kH16Threads * kH16Unroll);
+    const uint32_t pairs = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(want, (uint64_t)dev.sm_count / 2u));
+    ProfScope prof("hist16", st);
+    k_hist16<2><<<2u * pairs, kH16Threads, smem, st>>>(data, n, first_digit, d_counts, 1u);
+    return cudaPeekAtLastError() == cudaSuccess ? 0 : 5;
   }
   for (int d0 = 0; d0 < num_digits; d0 += 3) {
     const int nd = std::min(3, num_digits - d0);
@@ -458,7 +338,7 @@ int hist16(const Elem* data, uint32_t n, int first_digit, int num_digits, uint32
         1, std::min<uint64_t>(want, (uint64_t)dev.sm_count * per_sm));
     ProfScope prof("hist16", st);
     kern<<<grid, kH16Threads, smem, st>>>(data, n, first_digit + d0,
-                                          d_counts + (size_t)d0 * 65536u);
+                                          d_counts + (size_t)d0 * 65536u, 0u);
     if (cudaPeekAtLastError() != cudaSuccess) return 5;
   }
   return 0;
@@ -1070,7 +950,7 @@ int wide_run(Elem* X, Elem* Y, int first_digit, int target_parity, unsigned char
   unsigned char* wbase = ws + L.off_wide;
   DeviceInfo dev;
   if (int rc = current_device_info(&dev)) return rc;
-  if (int rc = hist16(X, L.n, first_digit, L.num_digits, hist, st, ctrl)) return rc;
+  if (int rc = hist16(X, L.n, first_digit, L.num_digits, hist, st)) return rc;
   {
     ProfScope prof("plan", st);
     k_plan16_scan<<<L.num_digits, kPlan16Threads, 0, st>>>(hist, gstart, L.n, ctrl);
