@@ -151,7 +151,7 @@ int plan_layout(int64_t n, int bits, int num_digits, Layout* L, bool allow_split
   L->n = (uint32_t)n;
   const size_t nbins = (size_t)1 << bits;
   size_t off = kCtrlBytes;
-  if (bits <= 11) {
+  if (bits <= kMaxOnesweepBits) {
     L->family = Family::kOnesweep;
     L->tile_elems = onesweep_tile_elems(bits);
     L->grid = onesweep_grid(bits, dev, L->n);
@@ -501,7 +501,7 @@ int lsb_histogram(const lsb_elem_t* d_data, int64_t n, int digit_bits, int64_t* 
   DeviceInfo dev;
   if (int rc = current_device_info(&dev)) return rc;
   const size_t smem = (size_t)P * nbins * 4u;
-  if (smem <= (size_t)dev.max_smem_optin && digit_bits <= 11) {
+  if (smem <= (size_t)dev.max_smem_optin && digit_bits <= kMaxOnesweepBits) {
     void* tmp = nullptr;
     if (int rc = pool_alloc(&tmp, smem, st)) return rc;
     int rc = histogram_u32(data, (uint32_t)n, digit_bits, 0, P, (uint32_t*)tmp, st);

@@ -13,6 +13,7 @@
 // digits with one bulk copy (16-byte stores for more than 256 digits).
 #include <algorithm>
 #include <cstdlib>
+#include <type_traits>
 
 #include "lsb_internal.h"
 
@@ -314,6 +315,63 @@ __device__ __forceinline__ void lookback_bins(const uint64_t* __restrict__ ring,
       }
     }
     if (any && !moved) {  // the nearest unconsumed predecessors have not published yet
+      if (++polls >= kSpinLimit || ((polls & 63u) == 0u && error_raised(ctrl))) {
+        record_error(ctrl, kStatusTimeout, kWhereLookback);
+        *timed_out = true;
+        break;
+      }
+      __nanosleep(ns);
+      if (ns < 256) ns <<= 1;
+    } else {
+      ns = 8;
+    }
+  }
+  *polls_out += polls;
+}
+
+// The same walk for NBT adjacent bins b0 .. b0 + NBT - 1 of one thread
+// (tile-tagged statuses): the bins' words of a predecessor share a sector, and
+// 32-bit tile indices with a bit mask of live bins keep the registers few.
+template <int NBT>
+__device__ __forceinline__ void lookback_adjacent(const uint64_t* __restrict__ ring,
+                                                  uint32_t ring_tiles, uint32_t nbins, uint32_t b0,
+                                                  int pass, uint32_t t, uint32_t* excl,
+                                                  uint64_t* mine, uint32_t tag,
+                                                  const uint32_t* count, Ctrl* ctrl,
+                                                  bool* timed_out, uint32_t* steps,
+                                                  uint32_t* polls_out) {
+  uint32_t j[NBT];
+#pragma unroll
+  for (int i = 0; i < NBT; i++) {
+    excl[i] = 0;
+    j[i] = t - 1u;
+  }
+  uint32_t live = t > 0 ? (1u << NBT) - 1u : 0u;
+  uint32_t polls = 0, ns = 8;
+  while (live) {
+    uint64_t s[NBT];
+#pragma unroll
+    for (int i = 0; i < NBT; i++)
+      if (live & (1u << i)) s[i] = ld_relaxed_u64(ring + (size_t)ring_slot(j[i], ring_tiles) * nbins + b0 + i);
+    *steps += 1;
+    bool moved = false;
+#pragma unroll
+    for (int i = 0; i < NBT; i++) {
+      if (live & (1u << i)) {
+        const uint64_t e = s[i];
+        if (status_tag(e) == ring_tag(pass, j[i]) && status_flag(e) != 0) {
+          excl[i] += (uint32_t)e;
+          moved = true;
+          if (status_flag(e) == kFlagIncl || j[i] == 0u) {
+            live &= ~(1u << i);
+            st_relaxed_u64(mine + b0 + i, pack_status(kFlagIncl, tag, excl[i] + count[b0 + i]));
+          } else {
+            j[i]--;
+          }
+        }
+      }
+    }
+    if (live && !moved) {  // the nearest unconsumed predecessors have not published yet
       if (++polls >= kSpinLimit || ((polls & 63u) == 0u && error_raised(ctrl))) {
         record_error(ctrl, kStatusTimeout, kWhereLookback);
         *timed_out = true;
@@ -690,6 +748,355 @@ __global__ void __launch_bounds__(THREADS, MINB)
   if (lb_polls) atomicAdd(&ctrl->lookback_polls, lb_polls);
 }
 
+// One pass for 9- to 12-bit digits (512 to 4096 bins), the tile ranked in
+// two steps instead of by per-warp counters of every bin. A stable sort of the
+// tile by its digit d = (h, l), l the low LB = ceil(b/2) bits, equals a stable
+// sort by l followed by a stable sort by h, so:
+//   1. rank the tile's items by l inside each warp (ballots, per-warp
+//      counters [2^LB][W+1]); every warp scans all warps' counters itself
+//      (no CTA barrier for the scan) and writes (d, original position) of
+//      each item to sk[] at its l-rank;
+//   2. read sk[] in order, rank by h the same way and count every digit of
+//      the tile (shared atomics); pos[original position] = final position;
+//   3. each thread owns 2^b / 512 consecutive bins: it publishes their tile
+//      counts, derives their tile-local starts (the start of h from step 2's
+//      counters plus a scan of the counts inside h, within a few lanes) and
+//      runs their decoupled look-back (tile-tagged statuses; the bins of a
+//      thread are adjacent words of the status row);
+//   4. stage the tile in digit order in shared memory, then 16-byte stores
+//      to the destination (runs average 2^13 / 2^b elements: too short for
+//      bulk copies).
+// Compared with per-warp counters of all 2^b bins ([2^b][17] per tile, summed
+// and scanned by every tile, then cleared), the counter work per tile is
+// (2^LB + 2^HB) x 17 plus one shared atomic per element. Measured on a GB300
+// (2^30 elements, 11-bit digits) it is nevertheless slower: 20.9 ms per pass
+// against 18.5 ms. Per tile about 57K cycles, of which the two ranking rounds
+// with their barriers take 27K, the look-back 13.5K and the 16-byte stores of
+// runs averaging four elements 9.5K, where the whole 8-bit tile takes 16.5K.
+// So it is a selectable variant (LSB_ONESWEEP_VARIANT=4), not the default.
+// Shared memory: stage E x 16 B, sk E x 4 B, pos E x 2 B, the two counter
+// sets, per-warp offset rows, tcount and goff (2^b x 4 B each).
+template <int BITS>
+__global__ void __launch_bounds__(512, 1)
+    k_onesweep2r(Elem* __restrict__ X, Elem* __restrict__ Y, uint32_t n, int, int pass, int digit,
+                 const uint32_t* __restrict__ gstart, uint64_t* __restrict__ ring,
+                 uint32_t* __restrict__ done, uint32_t ring_tiles, Ctrl* ctrl, SegDesc seg) {
+  constexpr int THREADS = 512, K = 16, W = THREADS / 32, WP = W + 1;
+  constexpr uint32_t E = THREADS * K;
+  constexpr int LB = (BITS + 1) / 2, HB = BITS - LB;
+  constexpr uint32_t NL = 1u << LB, NH = 1u << HB, NB = 1u << BITS;
+  constexpr uint32_t BPT = NB / THREADS;              // bins per thread (scan, look-back)
+  constexpr uint32_t TPG = NL / BPT;                  // threads per h group of bins
+  constexpr uint32_t BL = NL >= 32 ? NL / 32 : 1;     // step-1 bins per lane in the scan
+  constexpr uint32_t BH = NH >= 32 ? NH / 32 : 1;     // step-2 bins per lane in the scan
+  static_assert(BITS >= 9 && BITS <= 12, "two-step ranking covers 9- to 12-bit digits");
+  static_assert(TPG >= 1 && TPG <= 32 && NL % BPT == 0, "an h group lies inside one warp");
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ uint32_t s_tile, s_next;
+  __shared__ uint32_t s_err[2];
+
+  if (pass_skipped(ctrl, pass)) return;
+  const int shift = BITS * digit;
+  Elem* stage = reinterpret_cast<Elem*>(smem);                                    // [E]
+  uint32_t* sk = reinterpret_cast<uint32_t*>(smem + (size_t)E * 16u);             // [E]
+  uint16_t* pos = reinterpret_cast<uint16_t*>(smem + (size_t)E * 20u);            // [E]
+  uint32_t* tcount = reinterpret_cast<uint32_t*>(smem + (size_t)E * 22u);         // [NB]
+  uint32_t* goff = tcount + NB;                                                   // [NB]
+  uint32_t* o1w = goff + NB;                                                      // [W][NL]
+  uint32_t* o2w = o1w + W * NL;                                                   // [W][NH]
+  uint16_t* c1 = reinterpret_cast<uint16_t*>(o2w + W * NH);                       // [NL][WP]
+  uint16_t* c2 = c1 + ((NL * WP + 7u) & ~7u);                                     // [NH][WP]
+
+  const uint32_t par = ctrl->parity[pass];
+  const Elem* __restrict__ src = par ? Y : X;
+  Elem* __restrict__ dst = par ? X : Y;
+  const bool segmented = seg.tile_seg != nullptr;
+  const uint32_t num_tiles = segmented ? *seg.num_tiles : (n + E - 1) / E;
+  const uint32_t warp = threadIdx.x >> 5, lane = lane_id();
+  const uint32_t lt = lanemask_lt();
+  const uint32_t b0 = threadIdx.x * BPT;  // this thread's bins [b0, b0 + BPT)
+
+  struct TileInfo {
+    uint32_t begin, len, seg_base;
+    bool first;
+    const uint32_t* gs;
+  };
+  auto tile_info = [&](uint32_t t) {
+    TileInfo ti;
+    if (!segmented) {
+      ti.begin = t * E;
+      ti.len = min(E, n - ti.begin);
+      ti.seg_base = 0;
+      ti.first = t == 0;
+      ti.gs = gstart;
+    } else {
+      const uint32_t sg = seg.tile_seg[t];
+      const uint32_t j = t - seg.seg_tile0[sg];
+      const uint32_t sb = (uint32_t)seg.seg_off[sg], se = (uint32_t)seg.seg_off[sg + 1];
+      ti.begin = sb + j * E;
+      ti.len = min(E, se - ti.begin);
+      ti.seg_base = sb;
+      ti.first = j == 0;
+      ti.gs = seg.seg_gstart + ((size_t)sg * seg.num_passes + pass) * NB;
+    }
+    return ti;
+  };
+
+  Elem v[K];
+  auto load_tile = [&](uint32_t t) {
+    const TileInfo ti = tile_info(t);
+    const Elem* p = src + ti.begin + warp * 32u * K + lane;
+    if (ti.len == E) {
+#pragma unroll
+      for (int k = 0; k < K; k++) v[k] = load_elem_stream(p + k * 32);
+    } else {
+#pragma unroll
+      for (int k = 0; k < K; k++)
+        if (warp * 32u * K + (uint32_t)k * 32u + lane < ti.len) v[k] = load_elem_stream(p + k * 32);
+    }
+  };
+  // every warp's exclusive offsets of the `nb` bins of one ranking step, in
+  // [bin][warp] order, from all warps' counters c[bin][WP]: lane j sums bins
+  // j*bpl .. j*bpl + bpl - 1 over the warps, the warp scans the sums, and the
+  // row of this warp is written to o[bin]; hst[] receives the lane's bin starts
+  auto warp_offsets = [&](const uint16_t* c, uint32_t* o, uint32_t nb, auto bpl_tag, uint32_t* hst) {
+    constexpr uint32_t bpl = decltype(bpl_tag)::value;
+    uint32_t tot[bpl], part[bpl], sum = 0;
+#pragma unroll
+    for (uint32_t j = 0; j < bpl; j++) {
+      const uint32_t bin = lane * bpl + j;
+      uint32_t s = 0, p = 0;
+      if (bin < nb) {
+#pragma unroll
+        for (int w = 0; w < W; w++) {
+          const uint32_t x = c[bin * WP + w];
+          s += x;
+          p += (uint32_t)w < warp ? x : 0u;
+        }
+      }
+      tot[j] = s;
+      part[j] = p;
+      sum += s;
+    }
+    uint32_t inc = sum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, inc, o);
+      if (lane >= (uint32_t)o) inc += y;
+    }
+    uint32_t run = inc - sum;
+#pragma unroll
+    for (uint32_t j = 0; j < bpl; j++) {
+      const uint32_t bin = lane * bpl + j;
+      if (bin < nb) o[bin] = run + part[j];
+      hst[j] = run;
+      run += tot[j];
+    }
+    __syncwarp();
+  };
+
+  if (threadIdx.x == 0) s_tile = atomicAdd(&ctrl->ticket[pass], 1u);
+  for (uint32_t i = threadIdx.x; i < NL * WP; i += THREADS) c1[i] = 0;
+  for (uint32_t i = threadIdx.x; i < NH * WP; i += THREADS) c2[i] = 0;
+  for (uint32_t i = threadIdx.x; i < NB; i += THREADS) tcount[i] = 0;
+  __syncthreads();
+  uint32_t t = s_tile;
+  if (t < num_tiles) load_tile(t);
+  uint32_t lb_steps = 0, lb_polls = 0, iter = 0;
+
+  while (t < num_tiles) {
+    const TileInfo ti = tile_info(t);
+    const uint32_t len = ti.len;
+    const bool full = len == E;
+    const uint32_t slot = ring_slot(t, ring_tiles);
+    const uint32_t tag = ring_tag(pass, t);
+    uint32_t* err = &s_err[iter & 1u];
+    uint32_t ticket = 0;
+    if (threadIdx.x == 0) {
+      ticket = atomicAdd(&ctrl->ticket[pass], 1u);
+      *err = 0u;
+    }
+    // ring slot reuse: fetch the done tags of the old slot's readers now
+    const bool reuse = t >= ring_tiles;
+    const uint32_t x = t - ring_tiles;
+    uint32_t done_tag = 0;
+    const bool checker = reuse && threadIdx.x < gridDim.x && x + 1u + threadIdx.x < t;
+    if (checker) done_tag = ld_relaxed_u32(done + (x + 1u + threadIdx.x) % ring_tiles);
+
+    // 1. rank by the low LB bits inside each warp
+    uint32_t r1[K / 2];
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+      const uint32_t dl = (uint32_t)(v[k].key >> shift) & (NL - 1u);
+      const bool valid = full || warp * 32u * K + (uint32_t)k * 32u + lane < len;
+      const uint32_t peers = full ? warp_peers_fixed<LB>(dl) : warp_peers(dl, LB, valid);
+      uint16_t* cp = &c1[dl * WP + warp];
+      const uint32_t c = valid ? *cp : 0u;
+      const uint32_t r = c + __popc(peers & lt);
+      __syncwarp();
+      if (valid) *cp = (uint16_t)(c + __popc(peers));
+      __syncwarp();
+      if (k & 1) r1[k / 2] |= r << 16; else r1[k / 2] = r;
+    }
+    bool timed_out = false;
+    if (reuse) {
+      for (uint32_t j = 1u + threadIdx.x; j <= gridDim.x; j += THREADS) {
+        const uint32_t y = x + j;
+        if (y >= t) break;
+        const uint32_t got = (j == 1u + threadIdx.x) ? done_tag : ld_relaxed_u32(done + y % ring_tiles);
+        if (wait_done_tag(done + y % ring_tiles, ring_tag(pass, y), got, false, ctrl)) {
+          timed_out = true;
+          break;
+        }
+      }
+      if (checker) __threadfence();
+    }
+    if (threadIdx.x == 0) s_next = ticket;
+    __syncthreads();  // B1: step-1 counters complete
+    const uint32_t t_next = s_next;
+
+    // step-1 offsets of this warp; (digit, original position) to sk[] at the l-rank
+    {
+      uint32_t hst[BL];
+      warp_offsets(c1, o1w + warp * NL, NL, std::integral_constant<uint32_t, BL>{}, hst);
+#pragma unroll
+      for (int k = 0; k < K; k++) {
+        const uint32_t orig = warp * 32u * K + (uint32_t)k * 32u + lane;
+        if (full || orig < len) {
+          const uint32_t d = (uint32_t)(v[k].key >> shift) & (NB - 1u);
+          const uint32_t r = (k & 1) ? r1[k / 2] >> 16 : r1[k / 2] & 0xFFFFu;
+          sk[r + o1w[warp * NL + (d & (NL - 1u))]] = d | (orig << 16);
+        }
+      }
+    }
+    __syncthreads();  // B2: sk[] complete; every warp has read the step-1 counters
+    for (uint32_t b = lane; b < NL; b += 32u) c1[b * WP + warp] = 0;
+
+    // 2. rank by the high HB bits in l-sorted order; count every digit
+    uint32_t r2[K / 2];
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+      const uint32_t p = warp * 32u * K + (uint32_t)k * 32u + lane;
+      const bool valid = full || p < len;
+      const uint32_t e = valid ? sk[p] : 0u;
+      const uint32_t dh = (e & 0xFFFFu) >> LB;
+      const uint32_t peers = full ? warp_peers_fixed<HB>(dh) : warp_peers(dh, HB, valid);
+      uint16_t* cp = &c2[dh * WP + warp];
+      const uint32_t c = valid ? *cp : 0u;
+      const uint32_t r = c + __popc(peers & lt);
+      __syncwarp();
+      if (valid) {
+        *cp = (uint16_t)(c + __popc(peers));
+        atomicAdd(&tcount[e & 0xFFFFu], 1u);
+      }
+      __syncwarp();
+      if (k & 1) r2[k / 2] |= r << 16; else r2[k / 2] = r;
+    }
+    __syncthreads();  // B3: step-2 counters and the tile's digit counts complete
+
+    // 3. this thread's bins: publish the tile counts at once, then their
+    //    tile-local starts
+    uint64_t* my = ring + (size_t)slot * NB;
+    uint32_t ts[BPT];
+    {
+      uint32_t cnt[BPT], s = 0;
+#pragma unroll
+      for (uint32_t i = 0; i < BPT; i++) {
+        cnt[i] = tcount[b0 + i];
+        st_relaxed_u64(my + b0 + i, pack_status(ti.first ? kFlagIncl : kFlagAgg, tag, cnt[i]));
+        s += cnt[i];
+      }
+      uint32_t hst[BH];
+      warp_offsets(c2, o2w + warp * NH, NH, std::integral_constant<uint32_t, BH>{}, hst);
+      // start of h = b0 / NL (held by lane h / BH of this warp's step-2 scan)
+      const uint32_t h = b0 / NL;
+      uint32_t hs = 0;
+#pragma unroll
+      for (uint32_t j = 0; j < BH; j++) {
+        const uint32_t y = __shfl_sync(0xffffffffu, hst[j], (h / BH) & 31u);
+        if (h % BH == j) hs = y;
+      }
+      // exclusive scan of the counts inside the h group (TPG lanes)
+      uint32_t inc = s;
+#pragma unroll
+      for (uint32_t o = 1; o < TPG; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, inc, o);
+        if ((lane & (TPG - 1u)) >= o) inc += y;
+      }
+      uint32_t run = hs + inc - s;
+#pragma unroll
+      for (uint32_t i = 0; i < BPT; i++) {
+        ts[i] = run;
+        run += cnt[i];
+      }
+    }
+    // final position of every item, by its original position (sk[] read again)
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+      const uint32_t p = warp * 32u * K + (uint32_t)k * 32u + lane;
+      if (full || p < len) {
+        const uint32_t e = sk[p];
+        const uint32_t r = (k & 1) ? r2[k / 2] >> 16 : r2[k / 2] & 0xFFFFu;
+        pos[e >> 16] = (uint16_t)(r + o2w[warp * NH + ((e & 0xFFFFu) >> LB)]);
+      }
+    }
+    __syncthreads();  // B4: pos[] complete; every warp has read the step-2 counters
+    for (uint32_t b = lane; b < NH; b += 32u) c2[b * WP + warp] = 0;
+
+    // 4. stage the tile in digit order
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+      const uint32_t orig = warp * 32u * K + (uint32_t)k * 32u + lane;
+      if (full || orig < len) stage[pos[orig]] = v[k];
+    }
+    // decoupled look-back of this thread's bins -> destination offsets
+    {
+      uint32_t excl[BPT];
+#pragma unroll
+      for (uint32_t i = 0; i < BPT; i++) excl[i] = 0;
+      if (!ti.first)
+        lookback_adjacent<BPT>(ring, ring_tiles, NB, b0, pass, t, excl, my, tag, tcount, ctrl,
+                               &timed_out, &lb_steps, &lb_polls);
+#pragma unroll
+      for (uint32_t i = 0; i < BPT; i++) {
+        goff[b0 + i] = ti.seg_base + ti.gs[b0 + i] + excl[i] - ts[i];
+        tcount[b0 + i] = 0;
+      }
+    }
+    // the next tile's loads, into the registers freed by the staging
+    if (t_next < num_tiles) load_tile(t_next);
+    if (timed_out) *err = 1u;
+    __syncthreads();  // B5: staged, destinations known
+    if (threadIdx.x == 0 && ring_tiles < num_tiles) {
+      __threadfence();
+      st_release_u32(done + slot, tag);
+    }
+
+    // 5. the stores: position p of the digit-ordered tile goes to goff[d] + p
+    if (!*err) {
+      if (full) {
+#pragma unroll 4
+        for (int k = 0; k < K; k++) {
+          const uint32_t p = threadIdx.x + (uint32_t)k * THREADS;
+          const Elem e = stage[p];
+          const uint32_t o = goff[(uint32_t)(e.key >> shift) & (NB - 1u)] + p;
+          if (o < n) store_elem(dst + o, e);
+        }
+      } else {
+        for (uint32_t p = threadIdx.x; p < len; p += THREADS) {
+          const Elem e = stage[p];
+          const uint32_t o = goff[(uint32_t)(e.key >> shift) & (NB - 1u)] + p;
+          if (o < n) store_elem(dst + o, e);
+        }
+      }
+    }
+    t = t_next;
+    iter++;
+  }
+  if (lb_steps) atomicAdd(&ctrl->lookback_steps, lb_steps);
+  if (lb_polls) atomicAdd(&ctrl->lookback_polls, lb_polls);
+}
+
 // The same pass with the tile brought into shared memory by bulk copies (TMA,
 // cp.async.bulk completing on an mbarrier) instead of register loads, for up
 // to 256 digits. Elements do not occupy registers during the ranking, so a CTA
@@ -914,7 +1321,9 @@ __global__ void __launch_bounds__(THREADS, 1)
 // measured):
 //  1: bulk-copy kernel 768 x 8 (6144-element tiles, 24 warps) up to 256 digits;
 //  2: register kernel 256 x 16, two CTAs per SM;
-//  3: bulk-copy kernel 1024 x 4 (4096-element tiles, 32 warps) up to 256 digits.
+//  3: bulk-copy kernel 1024 x 4 (4096-element tiles, 32 warps) up to 256 digits;
+//  4: 9 to 11 bits by the two-step kernel k_onesweep2r (measured at 11 bits:
+//     20.9 ms per pass against 18.5 ms for the default).
 using OnesweepKernel = void (*)(Elem*, Elem*, uint32_t, int, int, int, const uint32_t*, uint64_t*,
                                 uint32_t*, uint32_t, Ctrl*, SegDesc);
 struct OnesweepChoice {
@@ -927,7 +1336,7 @@ struct OnesweepChoice {
 static int onesweep_variant() {
   const char* e = std::getenv("LSB_ONESWEEP_VARIANT");
   const int v = e ? std::atoi(e) : 0;
-  return (v >= 0 && v <= 3) ? v : 0;
+  return (v >= 0 && v <= 4) ? v : 0;
 }
 
 // staging buffer + per-warp counters + tstart[], gbase[] and tcount[]
@@ -938,12 +1347,23 @@ static size_t reg_kernel_smem(int bits, int threads, int k) {
   return E * sizeof(Elem) + onesweep_counter_bytes(nbins, threads / 32 + 1, cnt_bytes) +
          3u * (size_t)nbins * 4u;
 }
+// stage + sk + pos (22 B per element), tcount and goff, per-warp offset rows,
+// the two counter sets
+static size_t two_step_smem(int bits) {
+  const size_t E = 8192, W = 16, WP = 17;
+  const size_t NB = (size_t)1 << bits, NL = (size_t)1 << ((bits + 1) / 2), NH = NB / NL;
+  return 22u * E + 2u * NB * 4u + W * (NL + NH) * 4u + (((NL * WP + 7u) & ~(size_t)7u) + NH * WP) * 2u;
+}
 static size_t tma_kernel_smem(int threads, int k) {
   const size_t E = (size_t)threads * k;
   return 2u * E * sizeof(Elem) + (256u * (threads / 32 + 1) + 512u) * 4u;
 }
 
 static OnesweepChoice onesweep_choice(int bits, int v) {
+  if (bits >= 9 && bits <= kMaxOnesweepBits && v == 4) {
+    OnesweepKernel k = bits == 9 ? k_onesweep2r<9> : bits == 10 ? k_onesweep2r<10> : k_onesweep2r<11>;
+    return {k, 512, 8192, two_step_smem(bits)};
+  }
   if (bits <= 8 && (v == 1 || v == 3)) {
     if (v == 3)
       return {bits == 8 ? k_onesweep_tma<1024, 4, 8> : k_onesweep_tma<1024, 4, 0>, 1024, 4096,

@@ -35,11 +35,33 @@ def test_sort_matches_oracle(lsb, cuda, oracle, bits):
             assert np.array_equal(got, exp), (bits, dist, n)
 
 
-@pytest.mark.parametrize("bits", [1, 4, 5, 12, 13, 15])
+@pytest.mark.parametrize("bits", [1, 4, 5, 9, 10, 12, 13, 15])
 def test_other_digit_widths(lsb, cuda, oracle, bits):
     for dist in (0, 2, 4):
         a = oracle.generate(70001, dist, 3)
         assert np.array_equal(_sort(lsb, cuda, a, bits), oracle.stable_sort_by_key(a)), (bits, dist)
+
+
+@pytest.mark.parametrize("variant", ["0", "4"])
+@pytest.mark.parametrize("bits", [9, 10, 11])
+def test_wide_bin_onesweep(lsb, cuda, oracle, monkeypatch, bits, variant):
+    """Digits of 9 to 11 bits, one onesweep pass each: the default kernel
+    (per-warp counters of every digit) and the two-step kernel (the tile ranked
+    by the low half of the digit, then the high half; variant 4). Sizes at tile
+    edges, every distribution (equal keys: one bin per tile; Zipf: a few heavy
+    bins), and every single pass."""
+    monkeypatch.setenv("LSB_ONESWEEP_VARIANT", variant)
+    tile = 8192
+    for n in (1, 2, 31, tile - 1, tile, tile + 1, 3 * tile + 17, 40 * tile + 5):
+        for dist in DISTS:
+            a = oracle.generate(n, dist, n % 13)
+            assert np.array_equal(_sort(lsb, cuda, a, bits), oracle.stable_sort_by_key(a)), (bits, n, dist)
+    a = oracle.generate(5 * tile + 3, 0, 21)
+    src = to_dev(a, cuda)
+    for d in range(lsb.num_passes(bits)):
+        dst = cuda.empty_like(src)
+        lsb.global_shuffle(src, dst, d, bits)
+        assert np.array_equal(to_np(dst), oracle.global_shuffle(a, d, bits)), (bits, d)
 
 
 @pytest.mark.parametrize("bits", [16, 11, 8])
