@@ -288,8 +288,8 @@ int lsb_server_destroy(lsb_server_t* server);
  * lazy loading is the first call of this function on the device (that call
  * also loads the sort kernels), and it is held until the process exits.
  * So make the first call on each device at start-up, before an arena takes
- * the device's free memory and before any stream capture on it; a first
- * call that finds no memory left returns LSB_ERR_NO_MEMORY.
+ * the device's free memory; a first call that finds no memory left returns
+ * LSB_ERR_NO_MEMORY.
  * Limits: digit_bits 1..8, 12, 14 or 16 (a 12-, 14- or 16-bit digit runs as
  * two stable passes of half its width; other widths: LSB_ERR_INVALID_ARG)
  * and n up to LSB_MAX_ELEMENTS (LSB_ERR_TOO_LARGE); if the scratch this GPU's
