@@ -31,8 +31,8 @@ Prints ONE JSON line (rank 0):
                the same sort through the other digit widths and kernel
                families (all give the same bytes)
   histogram_b16
-               lsb_histogram at 16-bit digits: one HBM read by CTA pairs
-               against one read per three digits
+               lsb_histogram at 16-bit digits: one read per three digits
+               (default) against one HBM read by CTA pairs
 
 --impl reference times the reference algorithm on the host cores instead
 (see cpu_arm below). --gpus N (torchrun) runs N independent replicas, one
@@ -527,8 +527,8 @@ def gpu_arm(args, ranks: Ranks):
 
 def histogram_b16_leg(lsb, torch, data, reps: int = 3) -> dict:
     """lsb_histogram at 16-bit digits (four digits of every key) in its two
-    forms: CTA pairs over one HBM read of the keys (default), and one read per
-    three digits. Kernel time from the library's own launch events; the counts
+    forms: one read of the keys per three digits (default), and CTA pairs over
+    one HBM read. Kernel time from the library's own launch events; the counts
     of both forms must agree."""
     res, counts = {}, {}
     for form in ("pairs", "split"):

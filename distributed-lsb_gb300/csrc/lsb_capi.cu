@@ -516,7 +516,7 @@ int lsb_histogram(const lsb_elem_t* d_data, int64_t n, int digit_bits, int64_t* 
     return rc;
   }
   if (digit_bits == 16) {
-    // byte-packed counters: all four digits in one HBM read of the keys
+    // byte-packed counters, one read of the keys per three digits
     void* tmp = nullptr;
     const uint32_t cnt = (uint32_t)P * nbins;
     if (int rc = pool_alloc(&tmp, (size_t)cnt * 4u, st)) return rc;

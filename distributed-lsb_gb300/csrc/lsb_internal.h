@@ -90,8 +90,8 @@ int onesweep_pass_via(const Elem* src, Elem* mid, Elem* dst, int first_digit, un
 // that is cleared before every pass and *ring_bytes that of the status ring.
 size_t wide_layout_bytes(uint32_t n, size_t* pass_zero_bytes, size_t* ring_bytes, size_t offs[9]);
 // Counts of the 16-bit digits [first_digit, first_digit + num_digits) into
-// d_counts[num_digits][65536] (uint32): four digits in one HBM read of the
-// keys (CTA pairs), otherwise one read per three digits.
+// d_counts[num_digits][65536] (uint32): one read of the keys per three digits
+// (LSB_HIST16=pairs: four digits in one HBM read by CTA pairs).
 int hist16(const Elem* data, uint32_t n, int first_digit, int num_digits, uint32_t* d_counts,
            cudaStream_t st);
 

@@ -33,9 +33,8 @@
 // bounded (kSpinLimit polls): on expiry the kernel records
 // kStatusTimeout and returns.
 //
-// The digit counts come from hist16 (four digits in one HBM read of the keys
-// by CTA pairs, byte-packed shared-memory counters whose carries are repaired
-// in global memory).
+// The digit counts come from hist16 (byte-packed shared-memory counters
+// whose carries are repaired in global memory).
 //
 // Measured on a GB300 at 2^30 uniform elements: 76.7 ms per pass, against
 // 13.7 ms for the two 8-bit onesweep sub-passes of the default split, and
@@ -301,15 +300,15 @@ __global__ void __launch_bounds__(kH16Threads)
 }
 
 // Counts of 16-bit digits [first_digit, first_digit + num_digits) into
-// d_counts[num_digits][65536] (uint32; zeroed here). Four digits: one HBM read
-// of the keys by CTA pairs (two digits per CTA, the pair's second read of a
-// key served by L2); otherwise, or with LSB_HIST16=split, one read per three
-// digits. Both forms give the same counts in about the same time (7.7 and
-// 7.5 ms for four digits of 2^30 keys on a GB300: the counting instructions,
-// not the reads, bound both).
-static bool hist16_split() {
+// d_counts[num_digits][65536] (uint32; zeroed here): one read of the keys per
+// three digits, or with LSB_HIST16=pairs four digits in one HBM read by CTA
+// pairs (two digits per CTA, the pair's second read of a key served by L2).
+// Both give the same counts; the counting instructions, not the reads, bound
+// both, and the two reads measured faster (four digits of 2^30 keys on a
+// GB300: 7.53-7.55 ms against 7.72-8.42 ms for the pairs).
+static bool hist16_pairs() {
   const char* e = std::getenv("LSB_HIST16");
-  return e && std::strcmp(e, "split") == 0;
+  return e && std::strcmp(e, "pairs") == 0;
 }
 
 int hist16(const Elem* data, uint32_t n, int first_digit, int num_digits, uint32_t* d_counts,
@@ -318,7 +317,7 @@ int hist16(const Elem* data, uint32_t n, int first_digit, int num_digits, uint32
   if (int rc = current_device_info(&dev)) return rc;
   if (cudaMemsetAsync(d_counts, 0, (size_t)num_digits * 65536u * 4u, st) != cudaSuccess) return 5;
   if (n == 0) return 0;
-  if (num_digits == 4 && !hist16_split() && dev.sm_count >= 2) {
+  if (num_digits == 4 && hist16_pairs() && dev.sm_count >= 2) {
     const size_t smem = 2u * 65536u;
     if (cudaFuncSetAttribute(k_hist16<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
         cudaSuccess)
