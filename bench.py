@@ -67,6 +67,14 @@ def algorithmic_bytes_per_element(digit_bits: int, passes_run: int) -> int:
     return 8 + 32 * passes_run
 
 
+def workload_config(n: int, bits: int, dist: str, passes: int, world: int) -> dict:
+    """The `config` object of both arms: the workload the metric is quoted on."""
+    return {"workload": f"lsd-sort 2^{n.bit_length() - 1} {dist} u64 keys + u64 index values, "
+                        f"{bits}-bit digits ({passes} passes)",
+            "n": n, "digit_bits": bits, "dist": dist, "parallelism": f"replicas x{world}",
+            "l2": "inputs (16 B x n) far larger than L2; input restored by a 16 B x n copy before each step"}
+
+
 def args_parse(argv=None):
     p = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     p.add_argument("--gpus", type=int, default=1)
@@ -258,10 +266,11 @@ def cpu_arm(args, ranks: Ranks):
         "steps": len(times), "warmup": args.warmup, "ms_per_step": round(ms, 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
         "data": "synthetic",
-        "config": {"workload": f"lsd-sort uniform u64 keys, 16-bit digits, sample of {sample} elements per step",
-                   "n": sample, "digit_bits": 16, "dist": "uniform"},
+        # the native arm's workload; each step sorts a bounded sample of it
+        "config": workload_config(args.n, 16, "uniform", (64 + 15) // 16, ranks.world),
         "cpu_baseline": {"value": round(value, 3), "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": f"{sample} elements x {len(times)} steps"},
+                         "sample": f"{sample} uniform elements of the workload per step, 16-bit digits, "
+                                   f"{len(times)} timed steps, {threads} simulated ranks"},
         "e2e": {"value": round(value, 3), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
 
@@ -405,10 +414,7 @@ def gpu_arm(args, ranks: Ranks):
         "vs_baseline": None,
         "dtype": "u64",
         "data": "synthetic",
-        "config": {"workload": f"lsd-sort 2^{n.bit_length() - 1} {args.dist} u64 keys + u64 index values, "
-                               f"{bits}-bit digits ({passes_run} passes)",
-                   "n": n, "digit_bits": bits, "dist": args.dist, "parallelism": f"replicas x{ranks.world}",
-                   "l2": "inputs (16 B x n) far larger than L2; input restored by a 16 B x n copy before each step"},
+        "config": workload_config(n, bits, args.dist, passes_run, ranks.world),
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peaks["hbm_gbs"],
                      "unit": "GB/s", "frac": round(achieved / peaks["hbm_gbs"], 4),
                      "traffic": traffic, "traffic_source": traffic_src,
