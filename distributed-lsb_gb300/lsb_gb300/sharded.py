@@ -27,9 +27,10 @@ One pass (globalShuffle, :493-589), for digit d:
 
 Each rank sends and receives about (R-1)/R of its block per pass. The local
 step is the caller's: on GPUs the library's pass and histogram kernels
-(`GpuLocalOps`; received elements are placed by an index scatter); the
-exchange plan is plain integer arithmetic over the count table
-(`exchange_plan`), the same on every rank.
+(`GpuLocalOps`). The exchange plan is plain integer arithmetic over the count
+table (`exchange_plan`), the same on every rank; it describes what a rank
+receives as pieces (block-local destination, length), at most R x 2^b of
+them, and the pieces are expanded to element positions on the device.
 """
 from __future__ import annotations
 
@@ -48,9 +49,18 @@ def block_range(n: int, world: int, rank: int) -> tuple[int, int]:
 
 @dataclass
 class ExchangePlan:
-    send_counts: list[int]    # elements this rank sends to each rank, in rank order
-    recv_counts: list[int]    # elements this rank receives from each rank
-    recv_positions: np.ndarray  # block-local position of every received element, in arrival order
+    send_counts: list[int]   # elements this rank sends to each rank, in rank order
+    recv_counts: list[int]   # elements this rank receives from each rank
+    piece_dst: np.ndarray    # block-local start of every received piece, in arrival order
+    piece_len: np.ndarray    # length of every received piece
+
+    def positions(self) -> np.ndarray:
+        """Block-local position of every received element, in arrival order."""
+        total = int(self.piece_len.sum())
+        if total == 0:
+            return np.zeros(0, dtype=np.int64)
+        shift = self.piece_dst - np.concatenate(([0], np.cumsum(self.piece_len)[:-1]))
+        return np.repeat(shift, self.piece_len) + np.arange(total, dtype=np.int64)
 
 
 def exchange_plan(counts: np.ndarray, n: int, rank: int) -> ExchangePlan:
@@ -83,28 +93,26 @@ def exchange_plan(counts: np.ndarray, n: int, rank: int) -> ExchangePlan:
 
     send = [int(pieces(rank, q)[1].sum()) for q in range(world)]
     lo, _ = blocks[rank]
-    recv, pos = [], []
+    recv, dsts, lens = [], [], []
     for r in range(world):
         a, ln = pieces(r, rank)
         recv.append(int(ln.sum()))
-        if ln.size:
-            # the global positions a[i] .. a[i] + ln[i] - 1 of every piece, in order
-            rep = np.repeat(a - np.concatenate(([0], np.cumsum(ln)[:-1])), ln)
-            pos.append(rep + np.arange(int(ln.sum()), dtype=np.int64) - lo)
-    positions = np.concatenate(pos) if pos else np.zeros(0, dtype=np.int64)
-    return ExchangePlan(send, recv, positions)
+        dsts.append(a - lo)
+        lens.append(ln)
+    return ExchangePlan(send, recv, np.concatenate(dsts).astype(np.int64), np.concatenate(lens).astype(np.int64))
 
 
 class LocalOps:
     """The per-rank work of a pass. shuffle(block, digit, bits) returns the
     block stably sorted by the digit and the count of every digit value
-    (int64 numpy array of 2^bits); place(received, positions, size) returns a
-    block of `size` elements with received[i] at positions[i]."""
+    (int64 numpy array of 2^bits); place(received, plan, size) returns a block
+    of `size` elements with the received pieces at their destinations
+    (plan.piece_dst, plan.piece_len, in arrival order)."""
 
     def shuffle(self, block, digit: int, bits: int):
         raise NotImplementedError
 
-    def place(self, received, positions, size: int):
+    def place(self, received, plan: ExchangePlan, size: int):
         raise NotImplementedError
 
 
@@ -127,13 +135,20 @@ class GpuLocalOps(LocalOps):
             counts = np.zeros(1 << bits, dtype=np.int64)
         return out, counts
 
-    def place(self, received, positions, size: int):
+    def place(self, received, plan: ExchangePlan, size: int):
         import torch
 
-        out = torch.empty((size, 2), dtype=received.dtype, device=received.device)
-        if size:
-            idx = torch.from_numpy(positions).to(received.device)
-            out[idx] = received
+        dev = received.device
+        out = torch.empty((size, 2), dtype=received.dtype, device=dev)
+        total = received.shape[0]
+        if total:
+            # element positions from the piece table, on the device
+            lens = torch.from_numpy(plan.piece_len).to(dev)
+            starts = torch.cumsum(lens, 0) - lens
+            shift = torch.from_numpy(plan.piece_dst).to(dev) - starts
+            idx = torch.repeat_interleave(shift, lens, output_size=total)
+            idx += torch.arange(total, dtype=torch.int64, device=dev)
+            out.index_copy_(0, idx, received)
         return out
 
 
@@ -167,5 +182,5 @@ def sharded_sort(block, n: int, digit_bits: int, ops: LocalOps, dist, group=None
         recv = torch.empty((sum(plan.recv_counts), 2), dtype=block.dtype, device=dev)
         dist.all_to_all_single(recv, local.contiguous(), output_split_sizes=plan.recv_counts,
                                input_split_sizes=plan.send_counts, group=group)
-        block = ops.place(recv, plan.recv_positions, hi - lo)
+        block = ops.place(recv, plan, hi - lo)
     return block

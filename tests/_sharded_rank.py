@@ -26,9 +26,9 @@ class OracleLocalOps(sharded.LocalOps):
         out = oracle.global_shuffle(a, digit, bits)
         return torch.from_numpy(out.view(np.int64).copy()), oracle.histogram(a, bits)[digit].astype(np.int64)
 
-    def place(self, received, positions, size):
+    def place(self, received, plan, size):
         out = torch.empty((size, 2), dtype=torch.int64)
-        out[torch.from_numpy(positions)] = received
+        out[torch.from_numpy(plan.positions())] = received
         return out
 
 

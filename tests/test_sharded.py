@@ -41,8 +41,10 @@ def _simulate(oracle, a: np.ndarray, world: int, bits: int) -> np.ndarray:
             assert [sent[r][q].shape[0] for r in range(world)] == plans[q].recv_counts
             lo, hi = sharded.block_range(n, world, q)
             out = np.empty((hi - lo, 2), dtype=np.uint64)
-            out[plans[q].recv_positions] = recv
-            assert np.array_equal(np.sort(plans[q].recv_positions), np.arange(hi - lo))
+            pos = plans[q].positions()
+            out[pos] = recv
+            assert np.array_equal(np.sort(pos), np.arange(hi - lo))
+            assert plans[q].piece_dst.shape[0] <= world << bits
             new.append(out)
         blocks = new
     return np.concatenate(blocks)
@@ -85,3 +87,27 @@ def test_sharded_sort_gloo(oracle, world, n, dist, bits):
                 p.kill()
     for r, (rc, out, err) in enumerate(outs):
         assert rc == 0 and f"rank {r} ok" in out, (r, rc, out, err[-2000:])
+
+
+@pytest.mark.parametrize("world,bits", [(1, 8), (3, 8), (4, 16)])
+def test_piece_placement_expands_like_positions(world, bits):
+    """GpuLocalOps.place (piece table expanded with tensor ops, here on the
+    CPU) puts every received element where the plan's positions say."""
+    import torch
+
+    rng = np.random.default_rng(world * 100 + bits)
+    n = 5000 + world
+    counts = np.zeros((world, 1 << bits), dtype=np.int64)
+    for r in range(world):
+        lo, hi = sharded.block_range(n, world, r)
+        counts[r] = np.bincount(rng.integers(0, 1 << bits, size=hi - lo), minlength=1 << bits)
+    ops = sharded.GpuLocalOps(None, bits)
+    for q in range(world):
+        plan = sharded.exchange_plan(counts, n, q)
+        lo, hi = sharded.block_range(n, world, q)
+        total = sum(plan.recv_counts)
+        recv = torch.arange(2 * total, dtype=torch.int64).reshape(total, 2)
+        got = ops.place(recv, plan, hi - lo).numpy()
+        exp = np.empty((hi - lo, 2), dtype=np.int64)
+        exp[plan.positions()] = recv.numpy()
+        assert np.array_equal(got, exp), (world, bits, q)
