@@ -32,7 +32,7 @@ Prints ONE JSON line (rank 0):
                families (all give the same bytes)
   histogram_b16
                lsb_histogram at 16-bit digits: one read per three digits
-               (default) against one HBM read by CTA pairs
+               (default) against one HBM read by CTA pairs or quads
 
 --impl reference times the reference algorithm on the host cores instead
 (see cpu_arm below). --gpus N (torchrun) runs N independent replicas, one
@@ -532,12 +532,12 @@ def gpu_arm(args, ranks: Ranks):
 
 
 def histogram_b16_leg(lsb, torch, data, reps: int = 3) -> dict:
-    """lsb_histogram at 16-bit digits (four digits of every key) in its two
-    forms: one read of the keys per three digits (default), and CTA pairs over
-    one HBM read. Kernel time from the library's own launch events; the counts
-    of both forms must agree."""
+    """lsb_histogram at 16-bit digits (four digits of every key) in its three
+    forms: one read of the keys per three digits (default), and one HBM read by
+    CTA pairs (two digits each) or CTA quads (one digit each). Kernel time from
+    the library's own launch events; the counts of all forms must agree."""
     res, counts = {}, {}
-    for form in ("pairs", "split"):
+    for form in ("pairs", "quads", "split"):
         old = os.environ.get("LSB_HIST16")
         os.environ["LSB_HIST16"] = form
         try:
@@ -558,8 +558,8 @@ def histogram_b16_leg(lsb, torch, data, reps: int = 3) -> dict:
         launches, total = prof.get("hist16", (0, 0.0))
         counts[form] = h
         res[form] = {"ms": round(total / reps, 4), "launches": launches // reps,
-                     "hbm_reads_of_keys": 1 if form == "pairs" else 2}
-    res["counts_agree"] = bool(torch.equal(counts["pairs"], counts["split"]))
+                     "hbm_reads_of_keys": 2 if form == "split" else 1}
+    res["counts_agree"] = all(bool(torch.equal(counts[f], counts["split"])) for f in ("pairs", "quads"))
     return res
 
 

@@ -211,28 +211,28 @@ __device__ __forceinline__ void byte_flush(const uint32_t* words, uint32_t* g) {
 constexpr int kH16Threads = 512;
 constexpr int kH16Unroll = 8;
 
-// paired == 0: the CTAs share the whole array (grid-stride) and count digits
-// [first_digit, first_digit + ND). paired == 1: CTAs 2p and 2p+1 walk the
-// same contiguous range of the array side by side, CTA 2p counting digits
-// [first_digit, +ND) and CTA 2p+1 the ND digits after them, so that the
-// second read of every key is served by L2: 2*ND digits in one HBM read
-// without the shared memory for all of them in one CTA.
+// group == 1: the CTAs share the whole array (grid-stride) and count digits
+// [first_digit, first_digit + ND). group == G > 1: CTAs G*p .. G*p + G - 1
+// walk the same contiguous range of the array side by side, CTA G*p + r
+// counting the ND digits from first_digit + r*ND, so that L2 serves every
+// read of a key after the first: G*ND digits in one HBM read without the
+// shared memory for all of them in one CTA.
 template <int ND>
-__global__ void __launch_bounds__(kH16Threads)
+__global__ void __launch_bounds__(kH16Threads, ND == 1 ? 3 : 1)
     k_hist16(const Elem* __restrict__ data, uint32_t n, int first_digit,
-             uint32_t* __restrict__ ghist, uint32_t paired) {
+             uint32_t* __restrict__ ghist, uint32_t group) {
   extern __shared__ uint32_t cw[];  // [ND][16384]
   for (uint32_t i = threadIdx.x; i < ND * 16384u; i += blockDim.x) cw[i] = 0u;
   __syncthreads();
   const uint32_t lane = lane_id();
   const uint64_t chunk = 32u * kH16Unroll;
   uint64_t lo = 0, hi = n, warps_total, gw, threads_total, gt;
-  if (paired) {
-    const uint32_t role = blockIdx.x & 1u, pairs = gridDim.x >> 1, pair = blockIdx.x >> 1;
+  if (group > 1u) {
+    const uint32_t role = blockIdx.x % group, groups = gridDim.x / group, gi = blockIdx.x / group;
     first_digit += (int)role * ND;
     ghist += (size_t)role * ND * 65536u;
-    const uint64_t per = ((uint64_t)n + pairs - 1) / pairs;
-    lo = std::min<uint64_t>((uint64_t)pair * per, n);
+    const uint64_t per = ((uint64_t)n + groups - 1) / groups;
+    lo = std::min<uint64_t>((uint64_t)gi * per, n);
     hi = std::min<uint64_t>(lo + per, n);
     warps_total = blockDim.x >> 5;
     gw = threadIdx.x >> 5;
@@ -300,15 +300,35 @@ __global__ void __launch_bounds__(kH16Threads)
 }
 
 // Counts of 16-bit digits [first_digit, first_digit + num_digits) into
-// d_counts[num_digits][65536] (uint32; zeroed here): one read of the keys per
-// three digits, or with LSB_HIST16=pairs four digits in one HBM read by CTA
-// pairs (two digits per CTA, the pair's second read of a key served by L2).
-// Both give the same counts; the counting instructions, not the reads, bound
-// both, and the two reads measured faster (four digits of 2^30 keys on a
-// GB300: 7.53-7.55 ms against 7.72-8.42 ms for the pairs).
-static bool hist16_pairs() {
+// d_counts[num_digits][65536] (uint32; zeroed here). The default reads the
+// keys once per three digits; with four digits, LSB_HIST16 selects one HBM
+// read by groups of CTAs over the same range (L2 serves the group's other
+// reads): "pairs" (two digits per CTA, 128 KiB, one CTA per SM) or "quads"
+// (one digit per CTA, 64 KiB, three CTAs per SM). All give the same counts.
+static int hist16_group() {
   const char* e = std::getenv("LSB_HIST16");
-  return e && std::strcmp(e, "pairs") == 0;
+  if (e && std::strcmp(e, "pairs") == 0) return 2;
+  if (e && std::strcmp(e, "quads") == 0) return 4;
+  return 0;
+}
+
+template <int ND>
+static int hist16_grouped(const Elem* data, uint32_t n, int first_digit, uint32_t* d_counts,
+                          uint32_t group, const DeviceInfo& dev, cudaStream_t st) {
+  const size_t smem = (size_t)ND * 65536u;
+  if (cudaFuncSetAttribute(k_hist16<ND>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+      cudaSuccess)
+    return 5;
+  int per_sm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_hist16<ND>, kH16Threads, smem);
+  per_sm = std::max(per_sm, 1);
+  // enough groups to fill every resident slot, none with less than a few rounds of work
+  const uint64_t want = ((uint64_t)n + 8u * kH16Threads * kH16Unroll - 1) / (8u * kH16Threads * kH16Unroll);
+  const uint64_t slots = std::max<uint64_t>(1, (uint64_t)dev.sm_count * per_sm / group);
+  const uint32_t groups = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(want, slots));
+  ProfScope prof("hist16", st);
+  k_hist16<ND><<<group * groups, kH16Threads, smem, st>>>(data, n, first_digit, d_counts, group);
+  return cudaPeekAtLastError() == cudaSuccess ? 0 : 5;
 }
 
 int hist16(const Elem* data, uint32_t n, int first_digit, int num_digits, uint32_t* d_counts,
@@ -317,17 +337,9 @@ int hist16(const Elem* data, uint32_t n, int first_digit, int num_digits, uint32
   if (int rc = current_device_info(&dev)) return rc;
   if (cudaMemsetAsync(d_counts, 0, (size_t)num_digits * 65536u * 4u, st) != cudaSuccess) return 5;
   if (n == 0) return 0;
-  if (num_digits == 4 && hist16_pairs() && dev.sm_count >= 2) {
-    const size_t smem = 2u * 65536u;
-    if (cudaFuncSetAttribute(k_hist16<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
-        cudaSuccess)
-      return 5;
-    const uint64_t want = ((uint64_t)n + 8u * kH16Threads * kH16Unroll - 1) / (8u * kH16Threads * kH16Unroll);
-    const uint32_t pairs = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(want, (uint64_t)dev.sm_count / 2u));
-    ProfScope prof("hist16", st);
-    k_hist16<2><<<2u * pairs, kH16Threads, smem, st>>>(data, n, first_digit, d_counts, 1u);
-    return cudaPeekAtLastError() == cudaSuccess ? 0 : 5;
-  }
+  const int group = hist16_group();
+  if (num_digits == 4 && group == 2) return hist16_grouped<2>(data, n, first_digit, d_counts, 2u, dev, st);
+  if (num_digits == 4 && group == 4) return hist16_grouped<1>(data, n, first_digit, d_counts, 4u, dev, st);
   for (int d0 = 0; d0 < num_digits; d0 += 3) {
     const int nd = std::min(3, num_digits - d0);
     auto kern = nd == 3 ? k_hist16<3> : nd == 2 ? k_hist16<2> : k_hist16<1>;

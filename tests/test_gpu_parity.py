@@ -175,11 +175,11 @@ def test_histogram_matches_oracle(lsb, cuda, oracle):
             assert np.array_equal(h.cpu().numpy(), oracle.histogram(a, bits)), (bits, dist)
 
 
-@pytest.mark.parametrize("mode", ["pairs", "split"])
+@pytest.mark.parametrize("mode", ["pairs", "quads", "split"])
 def test_histogram_b16_forms(lsb, cuda, oracle, monkeypatch, mode):
-    """Both forms of the 16-bit count: CTA pairs over one HBM read, and one
-    read per three digits. Sizes cover a pair range with a partial round and
-    more pairs than the input needs."""
+    """Every form of the 16-bit count: one HBM read by CTA pairs or quads, and
+    one read per three digits. Sizes cover a group range with a partial round
+    and more groups than the input needs."""
     monkeypatch.setenv("LSB_HIST16", mode)
     for n, dist in ((1, 0), (4097, 1), (1 << 20, 0), (3 * (1 << 20) + 11, 2), (1 << 21, 4)):
         a = oracle.generate(n, dist, 9)
