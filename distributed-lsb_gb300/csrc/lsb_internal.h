@@ -91,7 +91,7 @@ int onesweep_pass_via(const Elem* src, Elem* mid, Elem* dst, int first_digit, un
 size_t wide_layout_bytes(uint32_t n, size_t* pass_zero_bytes, size_t* ring_bytes, size_t offs[9]);
 // Counts of the 16-bit digits [first_digit, first_digit + num_digits) into
 // d_counts[num_digits][65536] (uint32): one read of the keys per three digits
-// (LSB_HIST16=pairs: four digits in one HBM read by CTA pairs).
+// (LSB_HIST16=pairs or quads: four digits in one HBM read by groups of CTAs).
 int hist16(const Elem* data, uint32_t n, int first_digit, int num_digits, uint32_t* d_counts,
            cudaStream_t st);
 
