@@ -33,6 +33,8 @@ Prints ONE JSON line (rank 0):
   histogram_b16
                lsb_histogram at 16-bit digits: one read per three digits
                (default) against one HBM read by CTA pairs or quads
+  sharded      the sharded sort (block distribution, count all-gather and
+               element all-to-all per pass) over NCCL, 2^28 elements per rank
 
 --impl reference times the reference algorithm on the host cores instead
 (see cpu_arm below). --gpus N (torchrun) runs N independent replicas, one
@@ -105,6 +107,9 @@ def args_parse(argv=None):
     p.add_argument("--sweep-requests", type=int, default=1500)
     p.add_argument("--host-requests", type=int, default=1000)
     p.add_argument("--host-rate", type=float, default=1000.0)
+    p.add_argument("--no-sharded", action="store_true", help="skip the sharded-sort leg")
+    p.add_argument("--shard-n", type=int, default=1 << 28, help="elements per rank in the sharded leg")
+    p.add_argument("--shard-steps", type=int, default=3)
     return p.parse_args(argv)
 
 
@@ -519,6 +524,10 @@ def gpu_arm(args, ranks: Ranks):
     if not args.no_serving:
         out["serving"] = serving_leg(args, lsb, torch, ranks)
 
+    if not args.no_sharded:
+        torch.cuda.empty_cache()
+        out["sharded"] = sharded_leg(args, lsb, torch, ranks)
+
     if ranks.rank == 0 and ranks.world == 1 and not args.no_cpu:
         val, times, threads = cpu_sort_rate(args.cpu_sample, 3, warmup=1, budget_s=30.0)
         one = args.cpu_sample // 4
@@ -561,6 +570,80 @@ def histogram_b16_leg(lsb, torch, data, reps: int = 3) -> dict:
                      "hbm_reads_of_keys": 2 if form == "split" else 1}
     res["counts_agree"] = all(bool(torch.equal(counts[f], counts["split"])) for f in ("pairs", "quads"))
     return res
+
+
+def _unsigned_order(keys):
+    """int64 keys mapped so that signed comparison follows the unsigned order."""
+    return keys ^ (-(1 << 63))
+
+
+def _pair_checksum(torch, block):
+    """Sum (mod 2^64) of a mix of every key with its value: preserved exactly
+    when the sort only permutes whole elements."""
+    mixed = block[:, 0] ^ (block[:, 1] * -7046029254386353131)  # 0x9E3779B97F4A7C15 as int64
+    return mixed.sum()
+
+
+def sharded_leg(args, lsb, torch, ranks) -> dict:
+    """The sharded sort (lsb_gb300.sharded) over NCCL: args.shard_n elements
+    per rank (weak scaling), the reference's block distribution, one count
+    all-gather and one element all-to-all per pass, 16-bit digits. With one
+    GPU the group has a single rank, so the exchange is a copy to itself and
+    the leg measures the sharded machinery beside lsb_sort_pairs; under
+    torchrun every rank sorts with its own GPU. Checked by properties that
+    hold at any size: every block sorted, blocks in order across ranks, the
+    element count and a key-value checksum preserved."""
+    import socket
+
+    import torch.distributed as dist
+    from lsb_gb300 import sharded
+
+    own = ranks.dist is None
+    if own:
+        with socket.socket() as s:
+            s.bind(("127.0.0.1", 0))
+            port = s.getsockname()[1]
+        dist.init_process_group("nccl", init_method=f"tcp://127.0.0.1:{port}", rank=0, world_size=1)
+    try:
+        world, rank = dist.get_world_size(), dist.get_rank()
+        m, bits = args.shard_n, 16
+        n = m * world
+        block = lsb.generate(m, DIST_NAMES["uniform"], seed=1000 + rank)  # this rank's block
+        ops = sharded.GpuLocalOps(lsb, bits)
+        check_in = torch.stack([_pair_checksum(torch, block), torch.tensor(m, device=block.device)])
+        dist.all_reduce(check_in)
+        times, res = [], None
+        for i in range(1 + args.shard_steps):
+            dist.barrier()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            res = sharded.sharded_sort(block, n, bits, ops, dist)
+            torch.cuda.synchronize()
+            dt = time.perf_counter() - t0
+            t = torch.tensor([dt], dtype=torch.float64, device=block.device)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            if i >= 1:
+                times.append(float(t.item()))
+        keys = _unsigned_order(res[:, 0])
+        local_sorted = bool((keys[1:] >= keys[:-1]).all()) if keys.numel() > 1 else True
+        ends = torch.stack([keys[0], keys[-1]]) if keys.numel() else torch.zeros(2, dtype=torch.int64, device=keys.device)
+        all_ends = [torch.empty_like(ends) for _ in range(world)]
+        dist.all_gather(all_ends, ends)
+        ordered = all(int(all_ends[r][1]) <= int(all_ends[r + 1][0]) for r in range(world - 1))
+        flags = torch.tensor([0 if local_sorted else 1], device=keys.device)
+        dist.all_reduce(flags)
+        check_out = torch.stack([_pair_checksum(torch, res), torch.tensor(res.shape[0], device=res.device)])
+        dist.all_reduce(check_out)
+        ms = statistics.median(times) * 1e3
+        return {"n_per_rank": m, "world": world, "elements": n, "digit_bits": bits, "steps": len(times),
+                "ms_per_sort": round(ms, 3), "value": round(n / (ms / 1e3) / 1e6, 3), "unit": UNIT,
+                "scaling": "weak", "data": "uniform keys, one seeded stream per rank",
+                "sorted_check": bool(int(flags.item()) == 0 and ordered and torch.equal(check_in, check_out)),
+                "call": "lsb_gb300.sharded.sharded_sort with GpuLocalOps (lsb_pass + lsb_histogram per pass), "
+                        "NCCL all_gather of counts and all_to_all_single of elements"}
+    finally:
+        if own:
+            dist.destroy_process_group()
 
 
 def segmented_leg(args, lsb, torch, ranks) -> dict:
