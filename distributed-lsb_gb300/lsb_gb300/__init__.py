@@ -71,6 +71,9 @@ SIGNATURES = {
     "lsb_profile_read": (ctypes.c_int, [_P, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]),
     "lsb_selftest_wait_timeout": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int)]),
     "lsb_selftest_wait": (ctypes.c_int, [ctypes.c_int, _P, ctypes.POINTER(ctypes.c_int)]),
+    "lsb_exchange_plan": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int, _I64, ctypes.c_int, _P, _P, _P, _P, _P,
+                                         ctypes.POINTER(ctypes.c_int64)]),
+    "lsb_place_pieces": (ctypes.c_int, [_P, _I64, _P, _I64, _P, _P, _P, _I64, _P]),
 }
 
 
@@ -229,6 +232,41 @@ def histogram(data, digit_bits: int = 16, stream=None):
     _check(load().lsb_histogram(_ptr(data), data.shape[0], digit_bits, _ptr(out), _stream_ptr(stream)),
            "lsb_histogram")
     return out
+
+
+def exchange_plan(counts, n: int, rank: int):
+    """lsb_exchange_plan: the exchange of one pass of the sharded sort for
+    `rank` from the all-gathered count table counts[R][2^b] (int64 numpy).
+    Returns (send_counts, recv_counts, piece_src, piece_dst, piece_len), all
+    int64 numpy arrays (host computation, no GPU needed)."""
+    import numpy as np
+
+    c = np.ascontiguousarray(counts, dtype=np.int64)
+    ranks, nbins = c.shape
+    bits = nbins.bit_length() - 1
+    if nbins != 1 << bits:
+        raise ValueError("count table width must be a power of two")
+    send = np.zeros(ranks, np.int64)
+    recv = np.zeros(ranks, np.int64)
+    cap = max(1, ranks * nbins)
+    src, dst, ln = (np.zeros(cap, np.int64) for _ in range(3))
+    npieces = ctypes.c_int64(0)
+    ptr = lambda a: ctypes.c_void_p(a.ctypes.data)
+    _check(load().lsb_exchange_plan(ptr(c), ranks, bits, n, rank, ptr(send), ptr(recv), ptr(src), ptr(dst),
+                                    ptr(ln), ctypes.byref(npieces)), "lsb_exchange_plan")
+    k = npieces.value
+    return send, recv, src[:k].copy(), dst[:k].copy(), ln[:k].copy()
+
+
+def place_pieces(received, out, piece_src, piece_dst, piece_len, stream=None) -> None:
+    """lsb_place_pieces: out[piece_dst[i] .. + piece_len[i]) = received[piece_src[i] ..]
+    (CUDA int64 (m, 2) tensors; piece tables int64 numpy arrays)."""
+    import numpy as np
+
+    tabs = [np.ascontiguousarray(t, dtype=np.int64) for t in (piece_src, piece_dst, piece_len)]
+    ptrs = [ctypes.c_void_p(t.ctypes.data) for t in tabs]
+    _check(load().lsb_place_pieces(_ptr(received), received.shape[0], _ptr(out), out.shape[0], *ptrs,
+                                   len(tabs[0]), _stream_ptr(stream)), "lsb_place_pieces")
 
 
 def query(workspace, stream=None) -> Stats:

@@ -21,7 +21,7 @@ LIB_PATH = os.path.join(LIB_DIR, "liblsb.so")
 DRIVER_PATH = os.path.join(LIB_DIR, "lsb_sort")
 INCLUDE = os.path.join(REPO_ROOT, "include")
 
-CUDA_SOURCES = ["lsb_onesweep.cu", "lsb_wide.cu", "lsb_task.cu", "lsb_segmented.cu", "lsb_server.cu", "lsb_capi.cu", "lsb_noalloc.cu", "lsb_host.cu"]
+CUDA_SOURCES = ["lsb_onesweep.cu", "lsb_wide.cu", "lsb_task.cu", "lsb_segmented.cu", "lsb_server.cu", "lsb_capi.cu", "lsb_noalloc.cu", "lsb_host.cu", "lsb_sharded.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "--expt-relaxed-constexpr", "-Xcompiler", "-fPIC",
               "-I" + INCLUDE]

@@ -27,10 +27,11 @@ One pass (globalShuffle, :493-589), for digit d:
 
 Each rank sends and receives about (R-1)/R of its block per pass. The local
 step is the caller's: on GPUs the library's pass and histogram kernels
-(`GpuLocalOps`). The exchange plan is plain integer arithmetic over the count
-table (`exchange_plan`), the same on every rank; it describes what a rank
-receives as pieces (block-local destination, length), at most R x 2^b of
-them, and the pieces are expanded to element positions on the device.
+(`GpuLocalOps`). The exchange plan is integer arithmetic over the count table,
+the same on every rank, done by the library (lsb_exchange_plan): what a rank
+sends to each rank, and what it receives as pieces (offset in the received
+array, block-local destination, length), at most R x 2^b of them, which the
+library's placement kernel copies into place (lsb_place_pieces).
 """
 from __future__ import annotations
 
@@ -51,6 +52,7 @@ def block_range(n: int, world: int, rank: int) -> tuple[int, int]:
 class ExchangePlan:
     send_counts: list[int]   # elements this rank sends to each rank, in rank order
     recv_counts: list[int]   # elements this rank receives from each rank
+    piece_src: np.ndarray    # offset of every received piece in the received array
     piece_dst: np.ndarray    # block-local start of every received piece, in arrival order
     piece_len: np.ndarray    # length of every received piece
 
@@ -59,47 +61,21 @@ class ExchangePlan:
         total = int(self.piece_len.sum())
         if total == 0:
             return np.zeros(0, dtype=np.int64)
-        shift = self.piece_dst - np.concatenate(([0], np.cumsum(self.piece_len)[:-1]))
-        return np.repeat(shift, self.piece_len) + np.arange(total, dtype=np.int64)
+        return np.repeat(self.piece_dst - self.piece_src, self.piece_len) + np.arange(total, dtype=np.int64)
 
 
 def exchange_plan(counts: np.ndarray, n: int, rank: int) -> ExchangePlan:
     """The element exchange of one pass for `rank`, from the all-gathered count
-    table counts[r][v] (elements of digit value v in rank r's block).
+    table counts[r][v] (elements of digit value v in rank r's block), by the
+    library (lsb_exchange_plan, host arithmetic). Rank r's run of digit v
+    occupies the global range [start(v, r), start(v, r) + counts[r][v]) of the
+    pass's output, start digit-major over (v, r); the slice sent to rank q is
+    the part of every run inside q's block, runs in order, and the receiver
+    lays out what it gets the same way."""
+    from . import exchange_plan as native_plan
 
-    Rank r's run of digit v occupies the global range
-    [start(v, r), start(v, r) + counts[r][v]) of the pass's output, with
-    start digit-major over (v, r). Its locally sorted block is those runs in
-    order of v, so the slice sent to rank q is the part of every run inside
-    q's block, runs in order; the receiver lays out what it gets from rank r
-    the same way, which yields the position of each received element."""
-    counts = np.asarray(counts, dtype=np.int64)
-    world, nbins = counts.shape
-    totals = counts.sum(axis=0)
-    digit_start = np.concatenate(([0], np.cumsum(totals)[:-1]))           # [v]
-    rank_off = np.concatenate((np.zeros((1, nbins), np.int64), np.cumsum(counts, axis=0)[:-1]))  # [r][v]
-    run_start = digit_start[None, :] + rank_off                             # [r][v]
-    blocks = [block_range(n, world, q) for q in range(world)]
-
-    def pieces(r: int, q: int):
-        """(global start, length) of rank r's runs inside rank q's block, in run order."""
-        qlo, qhi = blocks[q]
-        s = run_start[r]
-        e = s + counts[r]
-        a = np.maximum(s, qlo)
-        b = np.minimum(e, qhi)
-        keep = b > a
-        return a[keep], (b - a)[keep]
-
-    send = [int(pieces(rank, q)[1].sum()) for q in range(world)]
-    lo, _ = blocks[rank]
-    recv, dsts, lens = [], [], []
-    for r in range(world):
-        a, ln = pieces(r, rank)
-        recv.append(int(ln.sum()))
-        dsts.append(a - lo)
-        lens.append(ln)
-    return ExchangePlan(send, recv, np.concatenate(dsts).astype(np.int64), np.concatenate(lens).astype(np.int64))
+    send, recv, src, dst, ln = native_plan(counts, n, rank)
+    return ExchangePlan([int(x) for x in send], [int(x) for x in recv], src, dst, ln)
 
 
 class LocalOps:
@@ -138,20 +114,10 @@ class GpuLocalOps(LocalOps):
     def place(self, received, plan: ExchangePlan, size: int):
         import torch
 
-        dev = received.device
-        total = received.shape[0]
-        starts = np.concatenate(([0], np.cumsum(plan.piece_len)[:-1])) if plan.piece_len.size else plan.piece_len
-        if total == size and np.array_equal(plan.piece_dst, starts):
+        if received.shape[0] == size and np.array_equal(plan.piece_dst, plan.piece_src):
             return received  # the pieces arrive in destination order (e.g. one rank): nothing to move
-        out = torch.empty((size, 2), dtype=received.dtype, device=dev)
-        if total:
-            # element positions from the piece table, on the device
-            lens = torch.from_numpy(plan.piece_len).to(dev)
-            starts = torch.cumsum(lens, 0) - lens
-            shift = torch.from_numpy(plan.piece_dst).to(dev) - starts
-            idx = torch.repeat_interleave(shift, lens, output_size=total)
-            idx += torch.arange(total, dtype=torch.int64, device=dev)
-            out.index_copy_(0, idx, received)
+        out = torch.empty((size, 2), dtype=received.dtype, device=received.device)
+        self.lsb.place_pieces(received, out, plan.piece_src, plan.piece_dst, plan.piece_len)
         return out
 
 

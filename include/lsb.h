@@ -276,6 +276,36 @@ int lsb_server_device_stats(lsb_server_t* server, lsb_server_device_stats_t* out
 /* Finishes every submitted request, then frees everything. */
 int lsb_server_destroy(lsb_server_t* server);
 
+/* Sharded sort over R processes (one GPU each), the reference's distributed
+ * structure: blocks of ceil(n / R) elements (DistributedArray,
+ * mpi/mpi_lsbsort.cpp:154-159). A pass is lsb_pass on the block (the local
+ * shuffle of localShuffle, :225-259), an all-gather of every rank's digit
+ * counts (lsb_histogram) by the caller's transport, then the two calls below
+ * around the caller's all-to-all of elements (:539-588).
+ *
+ * The exchange of one pass for `rank`, from the all-gathered count table
+ * counts[r * 2^b + v] (elements of digit value v in rank r's block; the
+ * counts must add up to n). It replaces copyCountsToGlobalCounts,
+ * exclusiveScan and copyStartsFromGlobalStarts (:339-491) and the element
+ * destinations (:558-575): the runs are placed digit-major over the ranks
+ * (GlobalCounts[digit * R + rank], :362). Outputs: send_counts[R] and
+ * recv_counts[R] (elements to and from each rank, for the all-to-all of the
+ * locally sorted block), and the received pieces in arrival order:
+ * piece_src[i] (offset in the received array), piece_dst[i] (block-local
+ * destination), piece_len[i]; *npieces of them, at most R * 2^b (the caller
+ * sizes the arrays). Host memory only, no GPU work. */
+int lsb_exchange_plan(const int64_t* counts, int ranks, int digit_bits, int64_t n, int rank,
+                      int64_t* send_counts, int64_t* recv_counts, int64_t* piece_src,
+                      int64_t* piece_dst, int64_t* piece_len, int64_t* npieces);
+
+/* Places the received pieces: d_out[piece_dst[i] .. + piece_len[i]) =
+ * d_recv[piece_src[i] .. + piece_len[i]). Piece tables in host memory (as
+ * lsb_exchange_plan returns them); every range is checked against recv_n and
+ * out_n before any GPU work (LSB_ERR_INVALID_ARG). Stream-ordered. */
+int lsb_place_pieces(const lsb_elem_t* d_recv, int64_t recv_n, lsb_elem_t* d_out, int64_t out_n,
+                     const int64_t* h_piece_src, const int64_t* h_piece_dst,
+                     const int64_t* h_piece_len, int64_t npieces, void* stream);
+
 /* Sort without any device allocation. No counterpart in the reference: it is
  * for callers that may not allocate device memory -- a host framework that
  * owns all GPU memory through its own arena, a latency-critical path that

@@ -63,6 +63,18 @@ def test_host_validation_without_gpu(lsb):
     # nothing to sort: succeeds without a device
     assert L.lsb_sort_pairs(null, null, 0, 16, null, 0, null) == lsb.LSB_OK
     assert L.lsb_sort_pairs(P(a), P(b), 1, 16, null, 0, null) == lsb.LSB_OK
+    # piece placement: every range is checked on the host before any GPU work
+    import numpy as np
+
+    src, dst, ln = (np.array(v, dtype=np.int64) for v in ([0, 5], [5, 0], [5, 5]))
+    ptrs = [P(t.ctypes.data) for t in (src, dst, ln)]
+    ln[1] = 6  # runs past the received array (the valid table is not passed: it would launch)
+    assert L.lsb_place_pieces(P(a), 10, P(b), 10, *ptrs, 2, null) == lsb.LSB_ERR_INVALID_ARG
+    ln[1], dst[0] = 5, 6  # runs past the block
+    assert L.lsb_place_pieces(P(a), 10, P(b), 10, *ptrs, 2, null) == lsb.LSB_ERR_INVALID_ARG
+    dst[0] = 5
+    assert L.lsb_place_pieces(P(a + 8), 10, P(b), 10, *ptrs, 2, null) == lsb.LSB_ERR_ALIGNMENT
+    assert L.lsb_place_pieces(P(a), 10, P(b), 10, *ptrs, 0, null) == lsb.LSB_OK  # no pieces
 
 
 def test_no_device_reports_status(lsb):

@@ -31,3 +31,55 @@ def test_sharded_sort_one_gpu(lsb, cuda, oracle):
                 assert np.array_equal(to_np(out), oracle.stable_sort_by_key(a)), (bits, kind, n)
     finally:
         dist.destroy_process_group()
+
+
+@pytest.mark.parametrize("world,bits", [(3, 8), (5, 16)])
+def test_place_pieces_matches_positions(lsb, cuda, world, bits):
+    """lsb_place_pieces puts every received piece where the plan says, for
+    plans of several ranks (pieces of every length, some empty ranks)."""
+    from lsb_gb300 import sharded
+
+    rng = np.random.default_rng(world + bits)
+    n = 40000 * world + 3
+    counts = np.zeros((world, 1 << bits), dtype=np.int64)
+    for r in range(world):
+        lo, hi = sharded.block_range(n, world, r)
+        counts[r] = np.bincount(np.minimum(rng.zipf(1.3, size=hi - lo) - 1, (1 << bits) - 1), minlength=1 << bits)
+    for q in range(world):
+        plan = sharded.exchange_plan(counts, n, q)
+        lo, hi = sharded.block_range(n, world, q)
+        total = sum(plan.recv_counts)
+        recv = cuda.arange(2 * total, dtype=cuda.int64, device="cuda").reshape(total, 2)
+        out = cuda.full((hi - lo, 2), -1, dtype=cuda.int64, device="cuda")
+        lsb.place_pieces(recv, out, plan.piece_src, plan.piece_dst, plan.piece_len)
+        exp = np.full((hi - lo, 2), -1, dtype=np.int64)
+        exp[plan.positions()] = recv.cpu().numpy()
+        assert np.array_equal(out.cpu().numpy(), exp), (world, bits, q)
+
+
+@pytest.mark.parametrize("world", [2, 3, 5])
+def test_sharded_ranks_simulated_on_one_gpu(lsb, cuda, oracle, world):
+    """Every rank of a sharded sort in one process on this GPU: each rank's
+    local lsb_pass and lsb_histogram, the element all-to-all as slicing of the
+    locally sorted blocks, and the library's placement kernel. The ranks run
+    one after another (nothing waits on another rank's kernel)."""
+    from lsb_gb300 import sharded
+
+    for bits, (kind, n) in ((16, (oracle.DIST_UNIFORM, 200003)), (8, (oracle.DIST_ZIPF, 90001)),
+                            (16, (oracle.DIST_NEARLY_SORTED, 65537))):
+        a = oracle.generate(n, kind, 4)
+        blocks = [to_dev(a[slice(*sharded.block_range(n, world, r))], cuda) for r in range(world)]
+        ops = sharded.GpuLocalOps(lsb, bits)
+        for digit in range(lsb.num_passes(bits)):
+            local, counts = zip(*(ops.shuffle(b, digit, bits) for b in blocks))
+            table = np.stack(counts)
+            plans = [sharded.exchange_plan(table, n, q) for q in range(world)]
+            sent = [cuda.split(local[r], plans[r].send_counts) for r in range(world)]
+            new = []
+            for q in range(world):
+                recv = cuda.cat([sent[r][q] for r in range(world)])
+                lo, hi = sharded.block_range(n, world, q)
+                new.append(ops.place(recv, plans[q], hi - lo))
+            blocks = new
+        got = np.concatenate([to_np(b) for b in blocks])
+        assert np.array_equal(got, oracle.stable_sort_by_key(a)), (world, bits, kind, n)

@@ -89,25 +89,71 @@ def test_sharded_sort_gloo(oracle, world, n, dist, bits):
         assert rc == 0 and f"rank {r} ok" in out, (r, rc, out, err[-2000:])
 
 
-@pytest.mark.parametrize("world,bits", [(1, 8), (3, 8), (4, 16)])
-def test_piece_placement_expands_like_positions(world, bits):
-    """GpuLocalOps.place (piece table expanded with tensor ops, here on the
-    CPU) puts every received element where the plan's positions say."""
-    import torch
+def _plan_reference(counts: np.ndarray, n: int, rank: int):
+    """The exchange plan restated with numpy (the checker of lsb_exchange_plan):
+    send and receive counts, and the received pieces (offset in the received
+    array, block-local destination, length) in arrival order."""
+    counts = np.asarray(counts, dtype=np.int64)
+    world, nbins = counts.shape
+    digit_start = np.concatenate(([0], np.cumsum(counts.sum(axis=0))[:-1]))
+    rank_off = np.concatenate((np.zeros((1, nbins), np.int64), np.cumsum(counts, axis=0)[:-1]))
+    run_start = digit_start[None, :] + rank_off
+    blocks = [sharded.block_range(n, world, q) for q in range(world)]
 
-    rng = np.random.default_rng(world * 100 + bits)
-    n = 5000 + world
-    counts = np.zeros((world, 1 << bits), dtype=np.int64)
+    def pieces(r, q):
+        qlo, qhi = blocks[q]
+        a = np.maximum(run_start[r], qlo)
+        b = np.minimum(run_start[r] + counts[r], qhi)
+        keep = b > a
+        return a[keep], (b - a)[keep]
+
+    send = [int(pieces(rank, q)[1].sum()) for q in range(world)]
+    lo = blocks[rank][0]
+    recv, dst, ln = [], [], []
     for r in range(world):
-        lo, hi = sharded.block_range(n, world, r)
-        counts[r] = np.bincount(rng.integers(0, 1 << bits, size=hi - lo), minlength=1 << bits)
-    ops = sharded.GpuLocalOps(None, bits)
-    for q in range(world):
-        plan = sharded.exchange_plan(counts, n, q)
-        lo, hi = sharded.block_range(n, world, q)
-        total = sum(plan.recv_counts)
-        recv = torch.arange(2 * total, dtype=torch.int64).reshape(total, 2)
-        got = ops.place(recv, plan, hi - lo).numpy()
-        exp = np.empty((hi - lo, 2), dtype=np.int64)
-        exp[plan.positions()] = recv.numpy()
-        assert np.array_equal(got, exp), (world, bits, q)
+        a, l_ = pieces(r, rank)
+        recv.append(int(l_.sum()))
+        dst.append(a - lo)
+        ln.append(l_)
+    dst, ln = np.concatenate(dst), np.concatenate(ln)
+    src = np.concatenate(([0], np.cumsum(ln)[:-1])) if ln.size else ln
+    return send, recv, src, dst, ln
+
+
+@pytest.mark.parametrize("world,bits", [(1, 8), (2, 4), (3, 8), (4, 16), (7, 5)])
+def test_native_plan_matches_reference(world, bits):
+    """lsb_exchange_plan (host code in the library) against the numpy restatement:
+    uniform, skewed and empty count tables, block sizes with a remainder."""
+    rng = np.random.default_rng(world * 31 + bits)
+    for kind in ("uniform", "skewed", "one_digit", "empty"):
+        n = 0 if kind == "empty" else 3001 * world + (world - 1)
+        counts = np.zeros((world, 1 << bits), dtype=np.int64)
+        for r in range(world):
+            lo, hi = sharded.block_range(n, world, r)
+            m = hi - lo
+            if kind == "uniform":
+                v = rng.integers(0, 1 << bits, size=m)
+            elif kind == "skewed":
+                v = np.minimum(rng.zipf(1.5, size=m) - 1, (1 << bits) - 1)
+            else:
+                v = np.full(m, (1 << bits) // 3)
+            counts[r] = np.bincount(v, minlength=1 << bits)
+        for q in range(world):
+            plan = sharded.exchange_plan(counts, n, q)
+            send, recv, src, dst, ln = _plan_reference(counts, n, q)
+            assert plan.send_counts == send and plan.recv_counts == recv, (world, bits, kind, q)
+            assert np.array_equal(plan.piece_src, src) and np.array_equal(plan.piece_dst, dst), (world, bits, kind, q)
+            assert np.array_equal(plan.piece_len, ln), (world, bits, kind, q)
+
+
+def test_native_plan_rejects_bad_tables():
+    """Counts that do not add up to n, negative counts, a rank outside the world."""
+    import lsb_gb300 as lsb
+
+    counts = np.array([[3, 1], [2, 2]], dtype=np.int64)
+    with pytest.raises(RuntimeError):
+        lsb.exchange_plan(counts, 9, 0)
+    with pytest.raises(RuntimeError):
+        lsb.exchange_plan(np.array([[3, -1], [2, 4]], dtype=np.int64), 8, 0)
+    with pytest.raises(RuntimeError):
+        lsb.exchange_plan(counts, 8, 2)
