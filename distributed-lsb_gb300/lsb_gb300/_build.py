@@ -19,6 +19,7 @@ BUILD_DIR = os.path.join(PKG_ROOT, "_build")
 LIB_DIR = os.path.join(PKG_ROOT, "lib")
 LIB_PATH = os.path.join(LIB_DIR, "liblsb.so")
 DRIVER_PATH = os.path.join(LIB_DIR, "lsb_sort")
+SHARD_SIM_PATH = os.path.join(LIB_DIR, "lsb_shard_sim")
 INCLUDE = os.path.join(REPO_ROOT, "include")
 
 CUDA_SOURCES = ["lsb_onesweep.cu", "lsb_wide.cu", "lsb_task.cu", "lsb_segmented.cu", "lsb_server.cu", "lsb_capi.cu", "lsb_noalloc.cu", "lsb_host.cu", "lsb_sharded.cu"]
@@ -80,6 +81,14 @@ def build(force: bool = False, verbose: bool = False) -> str:
         _run(["g++", "-O2", "-std=c++17", "-I" + INCLUDE, "-I" + HOST, "-I" + os.path.join(cuda, "include"),
               drv_src, "-o", DRIVER_PATH, "-L" + LIB_DIR, "-llsb", "-L" + os.path.join(cuda, "lib64"),
               "-lcudart", "-Wl,-rpath,$ORIGIN", "-Wl,-rpath," + os.path.join(cuda, "lib64")])
+    sim_src = os.path.join(HOST, "lsb_shard_sim.cpp")
+    sim_deps = [sim_src, os.path.join(HOST, "lsb_gb300.hpp"), os.path.join(INCLUDE, "lsb.h"), LIB_PATH]
+    if os.path.exists(sim_src) and (force or _stale(SHARD_SIM_PATH, sim_deps)):
+        cuda = _cuda_home()
+        _run(["g++", "-O2", "-std=c++17", "-pthread", "-I" + INCLUDE, "-I" + HOST,
+              "-I" + os.path.join(cuda, "include"), sim_src, "-o", SHARD_SIM_PATH, "-L" + LIB_DIR, "-llsb",
+              "-L" + os.path.join(cuda, "lib64"), "-lcudart", "-Wl,-rpath,$ORIGIN",
+              "-Wl,-rpath," + os.path.join(cuda, "lib64")])
     if verbose:
         print("built", LIB_PATH)
     return LIB_PATH

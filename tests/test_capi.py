@@ -103,3 +103,7 @@ def test_driver_command_line_without_gpu(lsb):
     assert r.returncode == 2 and "unknown --dist" in r.stderr
     r = subprocess.run([_build.DRIVER_PATH, "--n"], capture_output=True, text=True, timeout=60)
     assert r.returncode == 2 and "missing value" in r.stderr
+    # the sharded-sort simulation refuses bad arguments before any GPU work
+    for args in (["--ranks", "0"], ["--digit-bits", "17"], ["--bogus"], ["--n"]):
+        r = subprocess.run([_build.SHARD_SIM_PATH, *args], capture_output=True, text=True, timeout=60)
+        assert r.returncode == 2, (args, r.returncode, r.stderr)

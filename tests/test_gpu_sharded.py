@@ -83,3 +83,21 @@ def test_sharded_ranks_simulated_on_one_gpu(lsb, cuda, oracle, world):
             blocks = new
         got = np.concatenate([to_np(b) for b in blocks])
         assert np.array_equal(got, oracle.stable_sort_by_key(a)), (world, bits, kind, n)
+
+
+@pytest.mark.parametrize("ranks,n,bits,skew", [(1, 100003, 16, False), (2, 300007, 16, False),
+                                              (3, 200003, 8, True), (5, 65537, 11, False),
+                                              (8, 123457, 16, True), (4, 3, 8, False)])
+def test_cpp_sharded_sort_simulated_ranks(lsb, ranks, n, bits, skew):
+    """lsb_gb300::shardedSort (the C++ layer) with its ranks as host threads of
+    one process on this GPU (host/lsb_shard_sim.cpp): the result equals
+    std::stable_sort of the whole array, block by block in rank order."""
+    import subprocess
+
+    from lsb_gb300 import _build
+
+    cmd = [_build.SHARD_SIM_PATH, "--ranks", str(ranks), "--n", str(n), "--digit-bits", str(bits), "--seed", "7"]
+    if skew:
+        cmd.append("--skew")
+    r = subprocess.run(cmd, capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0 and r.stdout.strip().endswith("ok"), (r.returncode, r.stdout, r.stderr)
