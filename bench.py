@@ -128,10 +128,13 @@ class Ranks:
             import torch
             import torch.distributed as dist
 
+            from datetime import timedelta
+
             backend = "nccl" if torch.cuda.is_available() else "gloo"
             if backend == "nccl":
                 torch.cuda.set_device(self.local_rank)
-            dist.init_process_group(backend=backend)
+            # a rank that fails ends its peers' next collective within minutes
+            dist.init_process_group(backend=backend, timeout=timedelta(minutes=5))
             self.dist = dist
             self.backend = backend
 
