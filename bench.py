@@ -37,10 +37,10 @@ Prints ONE JSON line (rank 0):
                element all-to-all per pass) over NCCL, 2^28 elements per rank
 
 --impl reference times the reference algorithm on the host cores instead
-(see cpu_arm below). --gpus N (torchrun) runs N independent replicas, one
-2^30 sort per GPU per step ("replicas only": the single-array sort does not
-shard across the GPUs of one box here), value = elements of all ranks / max
-rank time.
+(see cpu_arm below). --gpus N (torchrun): the headline runs N independent
+replicas, one 2^30 sort per GPU per step, value = elements of all ranks / max
+rank time; the sharded leg sorts one array of N x 2^28 elements across the
+N ranks (an exchange per pass).
 """
 from __future__ import annotations
 
