@@ -43,13 +43,13 @@ def test_2p28_skew_and_stability(lsb, cuda, dist, skipped16):
     assert st.skipped_mask == skipped16
 
 
-@pytest.mark.parametrize("bits", [16, 8])
+@pytest.mark.parametrize("bits", [16, 11, 8])
 def test_2p30_uniform(lsb, cuda, bits):
     free, _ = cuda.cuda.mem_get_info()
     if free < 52 * 2**30:
         pytest.skip("needs ~50 GB of free device memory")
     bad, st = _sort_and_check(lsb, cuda, 1 << 30, lsb.DIST_UNIFORM, bits)
-    assert bad == 0 and st.passes_run == 64 // bits
+    assert bad == 0 and st.passes_run == lsb.num_passes(bits)
 
 
 @pytest.mark.parametrize("dist", [0, 2])
